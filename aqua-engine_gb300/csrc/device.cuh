@@ -1,0 +1,142 @@
+// device.cuh — the scene as the device sees it, and the traversal routine
+// shared by every kernel that casts rays (render wavefront, aqua_trace,
+// batched rendering).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "aq_math.h"
+
+namespace aq {
+
+struct DevMaterial {
+    float4 a;  // base colour rgb (linear), texture index (int bits, -1 none)
+    float4 b;  // metallic, roughness, specular, 0
+};
+struct DevLight {
+    float4 p0;  // xyz, type (int bits)
+    float4 e1;  // xyz, area
+    float4 e2;  // xyz, selection pmf
+    float4 le;  // radiance (quad, triangle) or intensity (point), cdf
+};
+struct DevTexture {
+    uint32_t offset;  // first texel in the texel pool
+    int32_t w, h;
+    int32_t pad;
+};
+struct DevCamera {
+    float pos[3], right[3], up[3], back[3];
+    float tan_half, aspect, lens_radius, focal;
+    int32_t width, height;
+};
+struct DevScene {
+    const float4* __restrict__ nodes;  // 4 words per node (bvh.h)
+    const float4* __restrict__ tris;   // 3 words per triangle, leaf order
+    const float2* __restrict__ uvs;    // 3 per triangle, leaf order
+    const DevMaterial* __restrict__ mats;
+    const DevLight* __restrict__ lights;
+    const DevTexture* __restrict__ texs;
+    const uint32_t* __restrict__ texels;  // RGBA8, sRGB
+    int32_t n_nodes, n_tris, n_mats, n_lights, n_texs;
+    float env[3];
+    DevCamera cam;
+};
+
+// Result of a traversal: leaf-order triangle index (or -1), its scene index,
+// distance and barycentrics.
+struct TraceResult {
+    float t, u, v;
+    int32_t tri;
+    int32_t id;
+};
+
+#if defined(__CUDACC__)
+
+template <class T>
+__device__ __forceinline__ T ldg_(const T* p) { return __ldg(p); }
+
+constexpr int kStackSize = 64;  // >= BVH depth (builder bound kBvhMaxDepth)
+
+// Stack-based traversal of the two-wide BVH (near child first, far child
+// pushed). ANY: stop at the first hit in (tmin, tmax). Otherwise the result is
+// the lexicographic minimum (t, scene index) over all triangles hit: boxes are
+// tested conservatively (slab_entry), a child is skipped only when its entry
+// distance exceeds the best t, so the answer does not depend on visit order.
+// COUNT: add inner-node visits and triangle tests to the counters.
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ TraceResult traverse(const DevScene& S, v3 o, v3 d, float tmin, float tmax,
+                                                uint32_t& n_nodes, uint32_t& n_tris) {
+    RayPre rp;
+    rp.o = o;
+    rp.invd = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+    rp.tmin = tmin;
+    rp.tmax = tmax;
+    RayShear sh = make_shear(o, d);
+    TraceResult r;
+    r.t = tmax; r.u = 0.0f; r.v = 0.0f; r.tri = -1; r.id = 0x7fffffff;
+    int32_t stack[kStackSize];
+    int sp = 0;
+    int32_t node = 0;
+    while (true) {
+        while (node >= 0) {
+            const float4* np = S.nodes + 4 * (size_t)node;
+            float4 w0 = ldg_(np), w1 = ldg_(np + 1), w2 = ldg_(np + 2);
+            int4 w3 = ldg_(reinterpret_cast<const int4*>(np + 3));
+            if (COUNT) ++n_nodes;
+            float t0 = slab_entry(w0.x, w0.y, w0.z, w0.w, w2.x, w2.y, rp, r.t);
+            float t1 = slab_entry(w1.x, w1.y, w1.z, w1.w, w2.z, w2.w, rp, r.t);
+            bool h0 = t0 != INFINITY, h1 = t1 != INFINITY;
+            if (h0 && h1) {
+                bool swap = t1 < t0;
+                int32_t nearc = swap ? w3.y : w3.x, farc = swap ? w3.x : w3.y;
+                stack[sp++] = farc;
+                node = nearc;
+            } else if (h0) {
+                node = w3.x;
+            } else if (h1) {
+                node = w3.y;
+            } else {
+                if (sp == 0) return r;
+                node = stack[--sp];
+            }
+        }
+        // Leaf.
+        int32_t code = ~node;
+        int32_t first = code >> 3, cnt = code & 7;
+        for (int k = 0; k < cnt; ++k) {
+            const float4* tp = S.tris + 3 * (size_t)(first + k);
+            float4 a = ldg_(tp), b = ldg_(tp + 1), c = ldg_(tp + 2);
+            if (COUNT) ++n_tris;
+            TriHit h = intersect_tri(sh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), tmin, tmax);
+            if (h.hit) {
+                int32_t id = __float_as_int(a.w);
+                if (ANY) {
+                    r.t = h.t; r.tri = first + k; r.id = id;
+                    return r;
+                }
+                if (h.t < r.t || (h.t == r.t && id < r.id)) {
+                    r.t = h.t; r.u = h.u; r.v = h.v; r.tri = first + k; r.id = id;
+                }
+            }
+        }
+        if (sp == 0) return r;
+        node = stack[--sp];
+    }
+}
+
+// Warp-aggregated append: lanes with pred set get consecutive slots of *ctr.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* ctr, bool pred) {
+    unsigned mask = __ballot_sync(__activemask(), pred);
+    if (!pred) return 0;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(ctr, (uint32_t)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+#endif  // __CUDACC__
+
+}  // namespace aq

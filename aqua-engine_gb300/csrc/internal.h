@@ -1,0 +1,112 @@
+// internal.h — the opaque handles behind the C ABI and the entry points the
+// CUDA translation units export to the ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/aqua.h"
+#include "bvh.h"
+#include "device.cuh"
+#include "scene.h"
+
+namespace aq {
+
+// Error carrying an aqua_status across internal layers; the ABI layer turns
+// it into a return code and aqua_last_error text.
+struct Error : std::runtime_error {
+    aqua_status status;
+    Error(aqua_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define AQ_CUDA(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            throw ::aq::Error(e_ == cudaErrorMemoryAllocation ? AQUA_ERR_OOM : AQUA_ERR_CUDA,  \
+                              std::string(#call) + ": " + cudaGetErrorString(e_));             \
+    } while (0)
+
+// Device buffer owned by a context; size in bytes.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+// Render workspace: path state and queues of the wavefront, sized on demand.
+struct Workspace {
+    size_t slots = 0;       // capacity in path slots
+    size_t buckets = 0;     // material buckets (materials + 1 for misses)
+    size_t pixels = 0;      // film capacity
+    DevBuf block;           // one allocation, carved below
+    float4* ray_o = nullptr;  // (o.xyz, tmin)
+    float4* ray_d = nullptr;  // (d.xyz, tmax)
+    float4* hit = nullptr;    // (t, u, v, leaf-order tri or -1)
+    float4* tp = nullptr;     // (throughput.rgb, pdf of the last BSDF sample)
+    uint4* pst = nullptr;     // (rng lo, rng hi, work index, depth)
+    uint32_t* q[2] = {nullptr, nullptr};
+    uint32_t* bucket = nullptr;  // buckets x slots
+    float4* sh_o = nullptr;   // (o.xyz, pixel bits)
+    float4* sh_d = nullptr;   // (d.xyz, tmax)
+    float4* sh_c = nullptr;   // (contribution.rgb, 0)
+    float4* film = nullptr;   // per-pixel sum
+    uint32_t* counters = nullptr;   // see kCnt*
+    unsigned long long* stats = nullptr;  // see kStat*
+    float* out_rgb = nullptr;  // staging for host films (pixels * 3)
+};
+
+enum { kCntQ0 = 0, kCntQ1 = 1, kCntShadow = 2, kCntBucket0 = 8 };
+enum { kStatExt = 0, kStatShadow, kStatPaths, kStatNodes, kStatTris, kStatShNodes, kStatShTris, kStatCount };
+
+}  // namespace aq
+
+struct aqua_scene {
+    aq::HostScene host;
+    aq::FlatBvh bvh;
+    void* pinned = nullptr;    // staged device image of the scene
+    bool pinned_is_cuda = false;
+    size_t bytes = 0;          // bytes of the device image
+    aq::DevBuf dev;            // device copy
+    aq::DevScene ds{};         // pointers into dev
+    bool uploaded = false;
+};
+
+struct aqua_ctx {
+    int device = 0;
+    bool host_only = false;    // AQUA_DEVICE_HOST_ONLY: loaders and exports only
+    int num_sms = 0;
+    int verbose = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    uint64_t alloc_count = 0;
+    uint64_t fail_alloc_after = 0;
+    aq::Workspace ws;
+    unsigned int* pinned_counter = nullptr;  // host-mapped copy of queue counts
+    std::vector<cudaEvent_t> events;         // pool for stage timing
+    aq::DevBuf trace_rays, trace_hits;       // staging for host-pointer traces
+    aq::DevBuf trace_stats;
+};
+
+namespace aq {
+
+// Device allocation through the context (honours the fail_alloc_after hook).
+void dev_alloc(aqua_ctx* ctx, DevBuf& b, size_t bytes);
+void dev_free(DevBuf& b);
+
+// Builds the device image of a scene (BVH, triangle words, materials,
+// lights, textures) in pinned memory and copies it to the device.
+void scene_build_device(aqua_ctx* ctx, aqua_scene* s);
+void scene_upload(aqua_ctx* ctx, aqua_scene* s);
+void scene_release(aqua_scene* s);
+DevCamera dev_camera(const aqua_camera& c);
+
+void trace_rays(aqua_ctx* ctx, aqua_scene* s, const aqua_ray* rays, size_t n, aqua_hit* out,
+                uint32_t flags, aqua_trace_counts* counts);
+void render_path(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg& cfg, const aqua_tuning& tune,
+                 float* rgb_out, uint32_t flags, aqua_stats* stats);
+void workspace_release(aqua_ctx* ctx);
+
+}  // namespace aq

@@ -1,0 +1,654 @@
+// render.cu — the wavefront path tracer.
+//
+// One iteration = three launches over compacted queues:
+//   k_trace_ext   closest hit for every active path; optionally bins the
+//                 path into a per-material queue (warp-aggregated atomics)
+//   k_shade       emission (MIS), next-event estimation (one shadow ray),
+//                 BSDF sampling, Russian roulette; a finished path is replaced
+//                 in place by the slot's next camera sample (ray generation)
+//   k_shadow      any-hit test of the shadow queue, film += unoccluded NEE
+// Path slot s owns pixels s, s + S, s + 2S, ... and runs their samples in
+// order, so film updates need no atomics and the image does not depend on
+// the launch shape, the slot count or the material sort.
+//
+// Light transport follows the reference's data semantics: camera
+// `Perspective` (scenes/cbox.json:516-543), `Principled` Lambert + GGX
+// (scenes/cbox.json:3-62), `Point` lights (scenes/cbox.json:544-561), quad
+// area lights (CornellBox-Original.mtl:80-87), `max_depth`
+// (scenes/integrator.json:5).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "internal.h"
+
+namespace aq {
+
+struct WaveParams {
+    uint64_t seed;
+    int32_t spp, spp_offset, max_depth, rr_depth;
+    uint32_t slots, pixels;
+    uint32_t nb;  // material buckets incl. the miss bucket (0 = unsorted)
+};
+
+struct WavePtrs {
+    float4* ray_o;
+    float4* ray_d;
+    float4* hit;
+    float4* tp;
+    uint4* pst;
+    uint32_t* q_in;
+    uint32_t* q_out;
+    uint32_t* bucket;
+    float4* sh_o;
+    float4* sh_d;
+    float4* sh_c;
+    float4* film;
+    uint32_t* counters;
+    unsigned long long* stats;
+};
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ v3 f3(float4 a) { return mk(a.x, a.y, a.z); }
+
+__device__ __forceinline__ uint32_t slot_work(const WaveParams& P, uint32_t s) {
+    if (s >= P.pixels) return 0;
+    uint32_t npix = (P.pixels - s + P.slots - 1) / P.slots;
+    return npix * (uint32_t)P.spp;
+}
+
+// Shirley-Chiu concentric square-to-disk mapping.
+__device__ __forceinline__ void concentric(float u, float v, float& x, float& y) {
+    float a = 2.0f * u - 1.0f, b = 2.0f * v - 1.0f;
+    if (a == 0.0f && b == 0.0f) { x = y = 0.0f; return; }
+    float r, phi;
+    if (fabsf(a) > fabsf(b)) { r = a; phi = (kPi / 4.0f) * (b / a); }
+    else { r = b; phi = (kPi / 2.0f) - (kPi / 4.0f) * (a / b); }
+    x = r * cosf(phi);
+    y = r * sinf(phi);
+}
+
+__device__ __forceinline__ void camera_ray(const DevCamera& c, uint32_t pixel, float u0, float u1, float u2,
+                                           float u3, v3& o, v3& d) {
+    uint32_t px = pixel % (uint32_t)c.width, py = pixel / (uint32_t)c.width;
+    float sx = (2.0f * (((float)px + u0) / (float)c.width) - 1.0f) * c.tan_half * c.aspect;
+    float sy = (1.0f - 2.0f * (((float)py + u1) / (float)c.height)) * c.tan_half;
+    v3 dc = mk(sx, sy, -1.0f), oc = mk(0, 0, 0);
+    if (c.lens_radius > 0.0f) {
+        float lx, ly;
+        concentric(u2, u3, lx, ly);
+        oc = mk(lx * c.lens_radius, ly * c.lens_radius, 0.0f);
+        dc = dc * c.focal - oc;
+    }
+    v3 R = mk(c.right[0], c.right[1], c.right[2]), U = mk(c.up[0], c.up[1], c.up[2]),
+       B = mk(c.back[0], c.back[1], c.back[2]);
+    o = mk(c.pos[0], c.pos[1], c.pos[2]) + R * oc.x + U * oc.y + B * oc.z;
+    d = normalize(R * dc.x + U * dc.y + B * dc.z);
+}
+
+__device__ __forceinline__ float draw(uint64_t& st, uint64_t inc) { return u01(pcg32_next(st, inc)); }
+
+// Starts work item j of slot s (pixel, sample), writing its camera ray.
+__device__ __forceinline__ bool start_path(const DevScene& S, const WaveParams& P, const WavePtrs& W,
+                                           uint32_t s, uint32_t j) {
+    if (j >= slot_work(P, s)) return false;
+    uint32_t pixel = s + (j / (uint32_t)P.spp) * P.slots;
+    uint32_t sample = (uint32_t)P.spp_offset + j % (uint32_t)P.spp;
+    uint64_t st = path_rng_state(P.seed, pixel, sample), inc = pixel_inc(pixel);
+    float u0 = draw(st, inc), u1 = draw(st, inc), u2 = draw(st, inc), u3 = draw(st, inc);
+    v3 o, d;
+    camera_ray(S.cam, pixel, u0, u1, u2, u3, o, d);
+    W.ray_o[s] = make_float4(o.x, o.y, o.z, 0.0f);
+    W.ray_d[s] = make_float4(d.x, d.y, d.z, INFINITY);
+    W.tp[s] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    W.pst[s] = make_uint4((uint32_t)st, (uint32_t)(st >> 32), j, 0u);
+    return true;
+}
+
+__device__ __forceinline__ float srgb_lut_lookup(const float* lut, uint32_t c) { return lut[c & 255u]; }
+
+__device__ __forceinline__ v3 texel(const DevScene& S, const DevTexture& T, int x, int y, const float* lut) {
+    x %= T.w; if (x < 0) x += T.w;
+    y %= T.h; if (y < 0) y += T.h;
+    uint32_t p = ldg_(S.texels + T.offset + (size_t)y * (size_t)T.w + (size_t)x);
+    return mk(srgb_lut_lookup(lut, p), srgb_lut_lookup(lut, p >> 8), srgb_lut_lookup(lut, p >> 16));
+}
+
+// Bilinear lookup with wrap addressing; texels are decoded to linear first.
+__device__ __forceinline__ v3 tex_bilinear(const DevScene& S, int ti, float u, float v, const float* lut) {
+    DevTexture T = S.texs[ti];
+    float x = u * (float)T.w - 0.5f, y = v * (float)T.h - 0.5f;
+    float fx = floorf(x), fy = floorf(y);
+    float ax = x - fx, ay = y - fy;
+    int ix = (int)fx, iy = (int)fy;
+    v3 c00 = texel(S, T, ix, iy, lut), c10 = texel(S, T, ix + 1, iy, lut);
+    v3 c01 = texel(S, T, ix, iy + 1, lut), c11 = texel(S, T, ix + 1, iy + 1, lut);
+    v3 a = c00 + (c10 - c00) * ax, b = c01 + (c11 - c01) * ax;
+    return a + (b - a) * ay;
+}
+
+__device__ __forceinline__ int pick_light(const DevScene& S, float u) {
+    int lo = 0, hi = S.n_lights - 1;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (u < S.lights[mid].le.w) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void film_add(float4* film, uint32_t pixel, v3 c) {
+    float4 f = film[pixel];
+    f.x += c.x; f.y += c.y; f.z += c.z;
+    film[pixel] = f;
+}
+
+// ---------------------------------------------------------------- kernels
+__global__ void k_raygen(DevScene S, WaveParams P, WavePtrs W) {
+    uint32_t n = min(P.slots, P.pixels);
+    uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid == 0) {
+        W.counters[kCntQ0] = n;
+        W.counters[kCntQ1] = 0;
+        W.counters[kCntShadow] = 0;
+    }
+    for (uint32_t s = tid; s < n; s += gridDim.x * blockDim.x) {
+        start_path(S, P, W, s, 0);
+        W.q_in[s] = s;
+    }
+}
+
+template <bool SORTED, bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_ext(DevScene S, WaveParams P, WavePtrs W, uint32_t cnt_in,
+                                                   uint32_t cnt_out) {
+    uint32_t n = W.counters[cnt_in];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        W.counters[cnt_out] = 0;
+        W.counters[kCntShadow] = 0;
+    }
+    uint32_t nodes = 0, tris = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t s = W.q_in[i];
+        float4 ro = W.ray_o[s], rd = W.ray_d[s];
+        TraceResult r = traverse<false, COUNT>(S, f3(ro), f3(rd), ro.w, rd.w, nodes, tris);
+        W.hit[s] = make_float4(r.t, r.u, r.v, __int_as_float(r.tri));
+        if (SORTED) {
+            uint32_t b = r.tri < 0 ? P.nb - 1
+                                   : ((uint32_t)__float_as_int(ldg_(S.tris + 3 * (size_t)r.tri + 1).w) & 0xffffu);
+            unsigned mask = __match_any_sync(__activemask(), b);
+            int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(&W.counters[kCntBucket0 + b], (uint32_t)__popc(mask));
+            base = __shfl_sync(mask, base, leader);
+            uint32_t pos = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+            W.bucket[(size_t)b * P.slots + pos] = s;
+        }
+    }
+    if (COUNT) {
+        for (int o = 16; o > 0; o >>= 1) {
+            nodes += __shfl_down_sync(0xffffffffu, nodes, o);
+            tris += __shfl_down_sync(0xffffffffu, tris, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&W.stats[kStatNodes], (unsigned long long)nodes);
+            atomicAdd(&W.stats[kStatTris], (unsigned long long)tris);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&W.stats[kStatExt], (unsigned long long)n);
+}
+
+template <bool SORTED>
+__global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtrs W, uint32_t cnt_in,
+                                               uint32_t cnt_out) {
+    __shared__ float lut[256];
+    __shared__ uint32_t prefix[257];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        float c = (float)i / 255.0f;
+        lut[i] = c <= 0.04045f ? c / 12.92f : powf((c + 0.055f) / 1.055f, 2.4f);
+    }
+    uint32_t n;
+    if (SORTED) {
+        if (threadIdx.x == 0) {
+            uint32_t acc = 0;
+            for (uint32_t b = 0; b < P.nb; ++b) {
+                prefix[b] = acc;
+                acc += W.counters[kCntBucket0 + b];
+            }
+            prefix[P.nb] = acc;
+        }
+        __syncthreads();
+        n = prefix[P.nb];
+    } else {
+        __syncthreads();
+        n = W.counters[cnt_in];
+    }
+    uint32_t* out_cnt = &W.counters[cnt_out];
+    unsigned long long done_paths = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t s;
+        if (SORTED) {
+            uint32_t lo = 0, hi = P.nb - 1;
+            while (lo < hi) {  // last bucket b with prefix[b] <= i
+                uint32_t mid = (lo + hi + 1) >> 1;
+                if (prefix[mid] <= i) lo = mid;
+                else hi = mid - 1;
+            }
+            s = W.bucket[(size_t)lo * P.slots + (i - prefix[lo])];
+        } else {
+            s = W.q_in[i];
+        }
+        uint4 ps = W.pst[s];
+        float4 tpv = W.tp[s];
+        float4 h = W.hit[s];
+        uint32_t j = ps.z, depth = ps.w;
+        uint32_t pixel = s + (j / (uint32_t)P.spp) * P.slots;
+        uint64_t st = (uint64_t)ps.x | ((uint64_t)ps.y << 32), inc = pixel_inc(pixel);
+        v3 thr = f3(tpv);
+        float pdf_b = tpv.w;
+        int32_t tri = __float_as_int(h.w);
+        bool cont = false;
+        if (tri < 0) {
+            v3 e = mk(S.env[0], S.env[1], S.env[2]);
+            if (e.x > 0.0f || e.y > 0.0f || e.z > 0.0f) film_add(W.film, pixel, thr * e);
+        } else {
+            float4 rd = W.ray_d[s];
+            const float4* tw = S.tris + 3 * (size_t)tri;
+            float4 a = ldg_(tw), b = ldg_(tw + 1), c = ldg_(tw + 2);
+            uint32_t info = (uint32_t)__float_as_int(b.w);
+            v3 v0 = f3(a), e1 = f3(b) - v0, e2 = f3(c) - v0;
+            v3 p = v0 + e1 * h.y + e2 * h.z;
+            v3 ng = normalize(cross(e1, e2));
+            v3 dir = f3(rd);
+            v3 wo = -dir;
+            int light = (int)(info >> 16) - 1;
+            if (light >= 0) {
+                DevLight L = S.lights[light];
+                v3 nl = normalize(cross(f3(L.e1), f3(L.e2)));
+                float cos_l = dot(nl, wo);
+                if (cos_l > 0.0f) {
+                    float w = 1.0f;
+                    if (depth > 0 && pdf_b > 0.0f) {
+                        float pl = L.e2.w * h.x * h.x / (L.e1.w * cos_l);
+                        w = power_heuristic(pdf_b, pl);
+                    }
+                    film_add(W.film, pixel, thr * f3(L.le) * w);
+                }
+            }
+            if ((int)depth < P.max_depth) {
+                if (dot(ng, wo) < 0.0f) ng = -ng;
+                DevMaterial m = S.mats[info & 0xffffu];
+                v3 base = f3(m.a);
+                int ti = __float_as_int(m.a.w);
+                if (ti >= 0) {
+                    const float2* uv = S.uvs + 3 * (size_t)tri;
+                    float2 t0 = ldg_(uv), t1 = ldg_(uv + 1), t2 = ldg_(uv + 2);
+                    float w0 = 1.0f - h.y - h.z;
+                    float tu = t0.x * w0 + t1.x * h.y + t2.x * h.z;
+                    float tv = t0.y * w0 + t1.y * h.y + t2.y * h.z;
+                    base = base * tex_bilinear(S, ti, tu, tv, lut);
+                }
+                Bsdf B = make_bsdf(base, m.b.x, m.b.y, m.b.z);
+                v3 T, Bt;
+                onb(ng, T, Bt);
+                v3 wol = mk(dot(wo, T), dot(wo, Bt), dot(wo, ng));
+                float u[kBounceDims];
+#pragma unroll
+                for (int k = 0; k < kBounceDims; ++k) u[k] = draw(st, inc);
+                // Next-event estimation: one light, one point, one shadow ray.
+                if (S.n_lights > 0 && wol.z > 0.0f) {
+                    DevLight L = S.lights[pick_light(S, u[0])];
+                    int ty = __float_as_int(L.p0.w);
+                    float pmf = L.e2.w;
+                    v3 contrib = mk(0, 0, 0), wi;
+                    float dist = 0.0f;
+                    if (ty == AQUA_LIGHT_POINT) {
+                        v3 dl = f3(L.p0) - p;
+                        float d2 = dot(dl, dl);
+                        dist = sqrtf(d2);
+                        wi = dl * (1.0f / dist);
+                        float cs = dot(wi, ng);
+                        if (cs > 0.0f && d2 > 0.0f) {
+                            v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
+                            contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs / (d2 * pmf));
+                        }
+                    } else {
+                        v3 le1 = f3(L.e1), le2 = f3(L.e2), xl;
+                        if (ty == AQUA_LIGHT_QUAD) {
+                            xl = f3(L.p0) + le1 * u[1] + le2 * u[2];
+                        } else {
+                            float su = sqrtf(u[1]);
+                            xl = f3(L.p0) + le1 * (su * (1.0f - u[2])) + le2 * (su * u[2]);
+                        }
+                        v3 nl = normalize(cross(le1, le2));
+                        v3 dl = xl - p;
+                        float d2 = dot(dl, dl);
+                        dist = sqrtf(d2);
+                        wi = dl * (1.0f / dist);
+                        float cl = -dot(wi, nl), cs = dot(wi, ng);
+                        if (cl > 0.0f && cs > 0.0f && d2 > 0.0f) {
+                            v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
+                            float pl = pmf * d2 / (L.e1.w * cl);
+                            float pb = bsdf_pdf(B, wol, wil);
+                            float w = power_heuristic(pl, pb);
+                            contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs * w / pl);
+                        }
+                    }
+                    if (contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f) {
+                        uint32_t k = warp_append(&W.counters[kCntShadow], true);
+                        v3 so = offset_ray(p, ng);
+                        W.sh_o[k] = make_float4(so.x, so.y, so.z, __int_as_float((int)pixel));
+                        W.sh_d[k] = make_float4(wi.x, wi.y, wi.z, dist * (1.0f - 1e-4f));
+                        W.sh_c[k] = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
+                    }
+                }
+                // BSDF sampling.
+                v3 wil = bsdf_sample(B, wol, u[3], u[4], u[5]);
+                if (wil.z > 0.0f && wol.z > 0.0f) {
+                    float pdf = bsdf_pdf(B, wol, wil);
+                    v3 f = bsdf_eval(B, wol, wil);
+                    if (pdf > 0.0f) {
+                        thr = thr * f * (wil.z / pdf);
+                        bool ok = maxc(thr) > 0.0f && isfinite(thr.x) && isfinite(thr.y) && isfinite(thr.z);
+                        if (ok && (int)depth >= P.rr_depth) {
+                            float q = fminf(1.0f, maxc(thr));
+                            if (u[6] >= q) ok = false;
+                            else thr = thr * (1.0f / q);
+                        }
+                        if (ok) {
+                            v3 wi = normalize(T * wil.x + Bt * wil.y + ng * wil.z);
+                            v3 no = offset_ray(p, ng);
+                            W.ray_o[s] = make_float4(no.x, no.y, no.z, 0.0f);
+                            W.ray_d[s] = make_float4(wi.x, wi.y, wi.z, INFINITY);
+                            W.tp[s] = make_float4(thr.x, thr.y, thr.z, pdf);
+                            W.pst[s] = make_uint4((uint32_t)st, (uint32_t)(st >> 32), j, depth + 1);
+                            cont = true;
+                        }
+                    }
+                }
+            }
+        }
+        if (!cont) {
+            ++done_paths;
+            cont = start_path(S, P, W, s, j + 1);
+        }
+        uint32_t k = warp_append(out_cnt, cont);
+        if (cont) W.q_out[k] = s;
+    }
+    for (int o = 16; o > 0; o >>= 1) done_paths += __shfl_down_sync(0xffffffffu, done_paths, o);
+    if ((threadIdx.x & 31) == 0 && done_paths) atomicAdd(&W.stats[kStatPaths], done_paths);
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_shadow(DevScene S, WaveParams P, WavePtrs W) {
+    uint32_t n = W.counters[kCntShadow];
+    if (blockIdx.x == 0)
+        for (uint32_t b = threadIdx.x; b < P.nb; b += blockDim.x) W.counters[kCntBucket0 + b] = 0;
+    uint32_t nodes = 0, tris = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 o = W.sh_o[i], d = W.sh_d[i];
+        TraceResult r = traverse<true, COUNT>(S, f3(o), f3(d), 0.0f, d.w, nodes, tris);
+        if (r.tri < 0) {
+            float4 c = W.sh_c[i];
+            film_add(W.film, (uint32_t)__float_as_int(o.w), mk(c.x, c.y, c.z));
+        }
+    }
+    if (COUNT) {
+        for (int o = 16; o > 0; o >>= 1) {
+            nodes += __shfl_down_sync(0xffffffffu, nodes, o);
+            tris += __shfl_down_sync(0xffffffffu, tris, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&W.stats[kStatShNodes], (unsigned long long)nodes);
+            atomicAdd(&W.stats[kStatShTris], (unsigned long long)tris);
+        }
+    }
+    if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&W.stats[kStatShadow], (unsigned long long)n);
+}
+
+__global__ void k_resolve(const float4* film, float* out, uint32_t pixels, float scale, int accumulate) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < pixels; p += gridDim.x * blockDim.x) {
+        float4 f = film[p];
+        if (accumulate) {
+            out[3 * (size_t)p + 0] += f.x;
+            out[3 * (size_t)p + 1] += f.y;
+            out[3 * (size_t)p + 2] += f.z;
+        } else {
+            out[3 * (size_t)p + 0] = f.x * scale;
+            out[3 * (size_t)p + 1] = f.y * scale;
+            out[3 * (size_t)p + 2] = f.z * scale;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- host side
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+static void ensure_workspace(aqua_ctx* ctx, size_t slots, size_t buckets, size_t pixels) {
+    Workspace& w = ctx->ws;
+    if (w.block.ptr && w.slots >= slots && w.buckets >= buckets && w.pixels >= pixels) return;
+    slots = std::max(slots, w.slots);
+    buckets = std::max(buckets, w.buckets);
+    pixels = std::max(pixels, w.pixels);
+    dev_free(w.block);
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
+    size_t o_ro = take(16 * slots), o_rd = take(16 * slots), o_hit = take(16 * slots), o_tp = take(16 * slots),
+           o_pst = take(16 * slots), o_q0 = take(4 * slots), o_q1 = take(4 * slots),
+           o_bk = take(4 * slots * std::max<size_t>(buckets, 1)), o_sho = take(16 * slots),
+           o_shd = take(16 * slots), o_shc = take(16 * slots), o_film = take(16 * pixels),
+           o_cnt = take(4 * (kCntBucket0 + std::max<size_t>(buckets, 1) + 8)), o_st = take(8 * 16),
+           o_out = take(12 * pixels);
+    dev_alloc(ctx, w.block, off);
+    char* b = (char*)w.block.ptr;
+    w.ray_o = (float4*)(b + o_ro); w.ray_d = (float4*)(b + o_rd); w.hit = (float4*)(b + o_hit);
+    w.tp = (float4*)(b + o_tp); w.pst = (uint4*)(b + o_pst);
+    w.q[0] = (uint32_t*)(b + o_q0); w.q[1] = (uint32_t*)(b + o_q1);
+    w.bucket = (uint32_t*)(b + o_bk);
+    w.sh_o = (float4*)(b + o_sho); w.sh_d = (float4*)(b + o_shd); w.sh_c = (float4*)(b + o_shc);
+    w.film = (float4*)(b + o_film);
+    w.counters = (uint32_t*)(b + o_cnt);
+    w.stats = (unsigned long long*)(b + o_st);
+    w.out_rgb = (float*)(b + o_out);
+    w.slots = slots; w.buckets = buckets; w.pixels = pixels;
+}
+
+void workspace_release(aqua_ctx* ctx) {
+    dev_free(ctx->ws.block);
+    ctx->ws = Workspace{};
+}
+
+template <class K>
+static int grid_for(aqua_ctx* ctx, K kernel, int block, int blocks_per_sm) {
+    int per_sm = blocks_per_sm;
+    if (per_sm <= 0) {
+        AQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0));
+        per_sm = std::max(per_sm, 1);
+    }
+    return ctx->num_sms * per_sm;
+}
+
+namespace {
+// Event pairs around launches of one stage, summed after the render.
+struct StageTimer {
+    aqua_ctx* ctx;
+    bool on;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pairs;
+    size_t* next;
+    cudaEvent_t get() {
+        if (*next >= ctx->events.size()) {
+            cudaEvent_t e;
+            AQ_CUDA(cudaEventCreate(&e));
+            ctx->events.push_back(e);
+        }
+        return ctx->events[(*next)++];
+    }
+    void begin() {
+        if (!on) return;
+        pairs.push_back({get(), nullptr});
+        AQ_CUDA(cudaEventRecord(pairs.back().first, ctx->stream));
+    }
+    void end() {
+        if (!on) return;
+        pairs.back().second = get();
+        AQ_CUDA(cudaEventRecord(pairs.back().second, ctx->stream));
+    }
+    double total_ms() {
+        double t = 0.0;
+        for (auto& p : pairs) {
+            float ms = 0.0f;
+            AQ_CUDA(cudaEventElapsedTime(&ms, p.first, p.second));
+            t += ms;
+        }
+        return t;
+    }
+};
+}  // namespace
+
+void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, const aqua_tuning& tune,
+                 float* rgb_out, uint32_t flags, aqua_stats* stats) {
+    const DevScene& S = sc->ds;
+    if (cfg.spp <= 0) throw Error(AQUA_ERR_INVALID_ARG, "spp must be positive");
+    if (cfg.max_depth < 0) throw Error(AQUA_ERR_INVALID_ARG, "max_depth must be >= 0");
+    size_t pixels = (size_t)S.cam.width * (size_t)S.cam.height;
+    if (pixels == 0 || pixels > (1u << 27)) throw Error(AQUA_ERR_INVALID_ARG, "resolution out of range");
+    if ((uint64_t)cfg.spp * (pixels + 1) > 0xFFFFFFFFull && tune.slots > 0 &&
+        (uint64_t)cfg.spp * ((pixels + tune.slots - 1) / tune.slots) > 0xFFFFFFFFull)
+        throw Error(AQUA_ERR_INVALID_ARG, "spp x pixels per slot exceeds 2^32");
+    size_t slots = tune.slots > 0 ? (size_t)tune.slots : std::min<size_t>(pixels, (size_t)1 << 21);
+    slots = std::min(slots, pixels);
+    if ((uint64_t)cfg.spp * ((pixels + slots - 1) / slots) > 0xFFFFFFFFull)
+        throw Error(AQUA_ERR_INVALID_ARG, "spp x pixels per slot exceeds 2^32");
+    bool sorted = tune.sort_by_material > 0 && S.n_mats + 1 <= 256;
+    size_t nb = sorted ? (size_t)S.n_mats + 1 : 0;
+    ensure_workspace(ctx, slots, nb, pixels);
+    Workspace& w = ctx->ws;
+    cudaStream_t st = ctx->stream;
+
+    WaveParams P;
+    P.seed = cfg.seed;
+    P.spp = cfg.spp;
+    P.spp_offset = cfg.spp_offset;
+    P.max_depth = cfg.max_depth;
+    P.rr_depth = cfg.rr_depth;
+    P.slots = (uint32_t)slots;
+    P.pixels = (uint32_t)pixels;
+    P.nb = (uint32_t)nb;
+    WavePtrs W;
+    W.ray_o = w.ray_o; W.ray_d = w.ray_d; W.hit = w.hit; W.tp = w.tp; W.pst = w.pst;
+    W.bucket = w.bucket; W.sh_o = w.sh_o; W.sh_d = w.sh_d; W.sh_c = w.sh_c; W.film = w.film;
+    W.counters = w.counters; W.stats = w.stats;
+
+    bool count = (flags & AQUA_RENDER_COUNT) != 0;
+    bool timing = (flags & AQUA_RENDER_STAGE_TIMING) != 0;
+    int bt = tune.block_trace > 0 ? tune.block_trace : 128;
+    int bs = tune.block_shade > 0 ? tune.block_shade : 128;
+    if (bt != 128 && bt != 64 && bt != 32) throw Error(AQUA_ERR_INVALID_ARG, "block_trace must be 32, 64 or 128");
+    if (bs != 128 && bs != 64 && bs != 32) throw Error(AQUA_ERR_INVALID_ARG, "block_shade must be 32, 64 or 128");
+
+    auto trace_k = sorted ? (count ? k_trace_ext<true, true> : k_trace_ext<true, false>)
+                          : (count ? k_trace_ext<false, true> : k_trace_ext<false, false>);
+    auto shade_k = sorted ? k_shade<true> : k_shade<false>;
+    auto shadow_k = count ? k_shadow<true> : k_shadow<false>;
+    int g_trace = grid_for(ctx, trace_k, bt, tune.blocks_per_sm);
+    int g_shade = grid_for(ctx, shade_k, bs, tune.blocks_per_sm);
+    int g_shadow = grid_for(ctx, shadow_k, bt, tune.blocks_per_sm);
+
+    cudaEvent_t ev0, ev1;
+    size_t next_event = 0;
+    StageTimer tt{ctx, timing, {}, &next_event}, ts{ctx, timing, {}, &next_event}, tsh{ctx, timing, {}, &next_event};
+    ev0 = tt.get();
+    ev1 = tt.get();
+
+    AQ_CUDA(cudaMemsetAsync(w.film, 0, 16 * pixels, st));
+    AQ_CUDA(cudaMemsetAsync(w.stats, 0, 8 * 16, st));
+    AQ_CUDA(cudaMemsetAsync(w.counters, 0, 4 * (kCntBucket0 + std::max<size_t>(nb, 1)), st));
+    AQ_CUDA(cudaEventRecord(ev0, st));
+    uint64_t launches = 0;
+    W.q_in = w.q[0];
+    W.q_out = w.q[1];
+    {
+        int g = (int)std::min<size_t>((std::min(slots, pixels) + 255) / 256, (size_t)ctx->num_sms * 16);
+        k_raygen<<<std::max(g, 1), 256, 0, st>>>(S, P, W);
+        AQ_CUDA(cudaGetLastError());
+        ++launches;
+    }
+    const int chunk = tune.iters_per_graph > 0 ? tune.iters_per_graph : 16;
+    uint64_t iter = 0;
+    unsigned int* pc = ctx->pinned_counter;
+    cudaEvent_t chunk_ev[2] = {tt.get(), tt.get()};
+    int c = 0;
+    const uint64_t max_iters = (uint64_t)(cfg.max_depth + 2) * (uint64_t)cfg.spp *
+                                   ((pixels + slots - 1) / slots) + 64;
+    while (true) {
+        for (int k = 0; k < chunk; ++k, ++iter) {
+            uint32_t in = (uint32_t)(iter & 1), out = 1u - in;
+            W.q_in = w.q[in];
+            W.q_out = w.q[out];
+            tt.begin();
+            trace_k<<<g_trace, bt, 0, st>>>(S, P, W, in, out);
+            tt.end();
+            ts.begin();
+            shade_k<<<g_shade, bs, 0, st>>>(S, P, W, in, out);
+            ts.end();
+            tsh.begin();
+            shadow_k<<<g_shadow, bt, 0, st>>>(S, P, W);
+            tsh.end();
+            launches += 3;
+        }
+        AQ_CUDA(cudaGetLastError());
+        AQ_CUDA(cudaMemcpyAsync(&pc[c & 1], &w.counters[iter & 1], 4, cudaMemcpyDeviceToHost, st));
+        AQ_CUDA(cudaEventRecord(chunk_ev[c & 1], st));
+        if (c > 0) {
+            AQ_CUDA(cudaEventSynchronize(chunk_ev[(c - 1) & 1]));
+            if (pc[(c - 1) & 1] == 0) break;
+        }
+        ++c;
+        if (iter > max_iters) {
+            AQ_CUDA(cudaStreamSynchronize(st));
+            if (pc[(c - 1) & 1] != 0)
+                throw Error(AQUA_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");
+            break;
+        }
+    }
+    float* dst = (flags & AQUA_RENDER_DEVICE_FILM) ? rgb_out : w.out_rgb;
+    bool acc = (flags & AQUA_RENDER_ACCUMULATE) != 0;
+    if (acc && !(flags & AQUA_RENDER_DEVICE_FILM))
+        AQ_CUDA(cudaMemcpyAsync(dst, rgb_out, 12 * pixels, cudaMemcpyHostToDevice, st));
+    {
+        int g = (int)std::min<size_t>((pixels + 255) / 256, (size_t)ctx->num_sms * 16);
+        k_resolve<<<g, 256, 0, st>>>(w.film, dst, (uint32_t)pixels, 1.0f / (float)cfg.spp, acc ? 1 : 0);
+        AQ_CUDA(cudaGetLastError());
+        ++launches;
+    }
+    AQ_CUDA(cudaEventRecord(ev1, st));
+    if (!(flags & AQUA_RENDER_DEVICE_FILM))
+        AQ_CUDA(cudaMemcpyAsync(rgb_out, w.out_rgb, 12 * pixels, cudaMemcpyDeviceToHost, st));
+    unsigned long long hs[16];
+    AQ_CUDA(cudaMemcpyAsync(hs, w.stats, 8 * 16, cudaMemcpyDeviceToHost, st));
+    AQ_CUDA(cudaStreamSynchronize(st));
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        float ms = 0.0f;
+        AQ_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        stats->device_ms = ms;
+        stats->paths = hs[kStatPaths];
+        stats->ext_rays = hs[kStatExt];
+        stats->shadow_rays = hs[kStatShadow];
+        stats->iterations = iter;
+        stats->trace_launches = iter;
+        stats->shade_launches = iter;
+        stats->shadow_launches = iter;
+        stats->total_launches = launches;
+        stats->node_visits = hs[kStatNodes];
+        stats->tri_tests = hs[kStatTris];
+        stats->shadow_node_visits = hs[kStatShNodes];
+        stats->shadow_tri_tests = hs[kStatShTris];
+        if (timing) {
+            stats->trace_ms = tt.total_ms();
+            stats->shade_ms = ts.total_ms();
+            stats->shadow_ms = tsh.total_ms();
+        }
+    }
+}
+
+}  // namespace aq

@@ -1,0 +1,320 @@
+"""Benchmark of the light-transport hot path.
+
+Workload (one "step"): the procedural Cornell box with GGX materials
+(roughness U[0.05,0.8], metallic {0,1} from seed 0), 1024 x 1024, 1024 spp,
+max depth 8, per-pixel PCG32 streams, fp32 film — 1,073,741,824 camera paths
+rendered by the wavefront kernels. Metric: Mpaths/s (higher is better).
+
+Arms:
+  default            libaqua on cuda:<local rank>; one JSON line from rank 0.
+  --impl reference   the reference has no runnable CPU path (src/lib.rs is
+                     empty), so the arm times the CPU oracle port (same
+                     estimator, FP32, all host threads) on a bounded sample of
+                     the same workload.
+
+Under torchrun (--gpus N > 1) every rank renders its own replica of the
+workload (the path shards by pixel with no exchange step), timing is the max
+over ranks and `value` is the sum of all ranks' paths over that time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "aqua-engine_gb300"))
+
+WORKLOAD = {"workload": "cornell-ggx-1024x1024-1024spp-depth8", "scene": "procedural Cornell box, GGX, seed 0",
+            "width": 1024, "height": 1024, "spp": 1024, "max_depth": 8, "rr_depth": 3, "film": "fp32"}
+METRIC = "Mpaths/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_sample_run(threads: int, target_s: float, seed: int = 0):
+    """Oracle port (FP32, `threads` host threads) on a band of rows of the
+    workload at full spp; returns (Mpaths/s, description)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import aqua
+    import pyoracle
+
+    hctx = aqua.Context(device=-2)
+    scene = hctx.procedural(2, seed=0, width=WORKLOAD["width"], height=WORKLOAD["height"])
+    orc = pyoracle.OracleScene.from_aqua(scene)
+    W = WORKLOAD["width"]
+    mid = (WORKLOAD["height"] // 2) * W
+    # calibrate on 64 pixels, then size the band for ~target_s seconds
+    t0 = time.perf_counter()
+    orc.render(WORKLOAD["spp"], WORKLOAD["max_depth"], seed=seed, precision=32, rr_depth=WORKLOAD["rr_depth"],
+               threads=threads, pixel_begin=mid, pixel_end=mid + 64)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    npx = int(max(64, min(W * 64, 64 * target_s / dt)))
+    t0 = time.perf_counter()
+    _, st = orc.render(WORKLOAD["spp"], WORKLOAD["max_depth"], seed=seed, precision=32,
+                       rr_depth=WORKLOAD["rr_depth"], threads=threads, pixel_begin=mid, pixel_end=mid + npx)
+    dt = time.perf_counter() - t0
+    paths = float(st[0])
+    scene.free()
+    hctx.close()
+    return paths / dt / 1e6, dt, f"{npx} pixels from the middle row of the 1024x1024 image, 1024 spp each " \
+                                  f"({int(paths)} paths, {dt:.1f} s)"
+
+
+def run_reference(args, world, rank, pg):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample_run(threads, 1.0)
+    vals, secs = [], []
+    desc = ""
+    for _ in range(args.steps):
+        v, dt, desc = cpu_sample_run(threads, 10.0)
+        vals.append(v)
+        secs.append(dt)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(secs),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (procedural scene, seeded)", "config": dict(WORKLOAD, parallelism="cpu threads"),
+            "cpu_baseline": {"value": value, "unit": "Mpaths/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference crate has no implementation (src/lib.rs is empty); this arm times the CPU "
+                    "oracle port of the same estimator"}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, world, rank, local, pg):
+    import aqua
+
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    ctx = aqua.Context(device=local)
+    scene = ctx.procedural(2, seed=0, width=WORKLOAD["width"], height=WORKLOAD["height"])
+    info = scene.info()
+    cfg = ctx.integrator(spp=WORKLOAD["spp"], max_depth=WORKLOAD["max_depth"], rr_depth=WORKLOAD["rr_depth"],
+                         seed=1)
+    tune = ctx.tuning()
+    import torch
+
+    torch.cuda.set_device(local)
+    film = torch.zeros(info.width * info.height * 3, dtype=torch.float32, device=f"cuda:{local}")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")  # > 129 MB L2
+    torch.cuda.synchronize()
+
+    # Untimed counting pass: node visits and triangle tests of this exact
+    # workload (deterministic, so every timed step repeats them).
+    cst = ctx.render_device(scene, cfg, film.data_ptr(), tune, flags=aqua.RENDER_COUNT)
+    for _ in range(args.warmup):
+        ctx.render_device(scene, cfg, film.data_ptr(), tune)
+
+    barrier(pg)
+    torch.cuda.synchronize()
+    steps = []
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            steps.append(ctx.render_device(scene, cfg, film.data_ptr(), tune, flags=aqua.RENDER_STAGE_TIMING))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    barrier(pg)
+    dev_ms = sum(s.device_ms for s in steps)
+    ms_max = max_over_ranks(pg, dev_ms)
+    paths = sum(s.paths for s in steps)
+    all_paths = sum_over_ranks(pg, paths)
+    value = all_paths / (ms_max * 1e-3) / 1e6
+
+    # Dominant kernel: closest-hit traversal.
+    trace_ms = sum(s.trace_ms for s in steps)
+    launches = sum(s.trace_launches for s in steps)
+    ext = cst.ext_rays
+    bytes_step = cst.node_visits * 64 + cst.tri_tests * 48 + ext * (32 + 16)
+    bytes_per_launch = bytes_step / max(cst.trace_launches, 1)
+    avg_launch_s = trace_ms * 1e-3 / max(launches, 1)
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": args.traffic_per_launch, "peak_source": peak_src,
+                "kernel": "k_trace_ext (closest-hit BVH traversal)",
+                "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6,
+                "note": "algorithmic bytes = node visits x 64 B + triangle tests x 48 B + 48 B per ray; "
+                        "the Cornell BVH (19 nodes) is cache-resident, so DRAM traffic is far below this"}
+
+    # End to end through the C ABI with host buffers: scene upload + render
+    # + film download every step.
+    host_film = None
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier(pg)
+    t0 = time.perf_counter()
+    e2e_paths = 0
+    for _ in range(e2e_steps):
+        scene.upload()
+        host_film, st = ctx.render(scene, cfg, tune, out=host_film)
+        e2e_paths += st.paths
+    e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
+    e2e_value = sum_over_ranks(pg, e2e_paths) / e2e_s / 1e6
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, dt, desc = cpu_sample_run(threads, args.cpu_seconds)
+        cpu = {"value": v, "unit": "Mpaths/s", "cores": threads, "kind": "port", "sample": desc}
+
+    gpu_launches = sum(s.total_launches for s in steps)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (procedural Cornell box, seeded)",
+                "config": dict(WORKLOAD, parallelism=f"replicas x{world}",
+                               l2="256 MB buffer zeroed before every timed step; wavefront state "
+                                  f"{ctx.workspace_bytes() / 1e6:.0f} MB > 129 MB L2"),
+                "mrays_per_s": sum_over_ranks(pg, sum(s.ext_rays + s.shadow_rays for s in steps)) /
+                               (ms_max * 1e-3) / 1e6,
+                "wall_s": wall, "clocks": clk.summary(), "roofline": roofline, "cpu_baseline": cpu,
+                "e2e": {"value": e2e_value, "unit": "Mpaths/s", "h2d_bytes_per_step": int(info.upload_bytes),
+                        "d2h_bytes_per_step": int(info.width * info.height * 12)},
+                "gpu_launches": gpu_launches,
+                "stage_ms_per_step": {"trace": trace_ms / args.steps,
+                                      "shade": sum(s.shade_ms for s in steps) / args.steps,
+                                      "shadow": sum(s.shadow_ms for s in steps) / args.steps}}
+        print(json.dumps(line), flush=True)
+    scene.free()
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="aqua", choices=["aqua", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--traffic-per-launch", type=float, default=None,
+                    help="DRAM bytes per k_trace_ext launch from an ncu capture")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warning: fewer than 3 warm-up steps")
+    world, rank, local, pg = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, world, rank, pg)
+    else:
+        run_gpu(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

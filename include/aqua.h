@@ -1,0 +1,307 @@
+/*
+ * aqua.h — C ABI of libaqua, the GB300 (sm_103a) light-transport hot path.
+ *
+ * The reference crate (`arukas`, Cargo.toml:2-5) never wrote its renderer API:
+ * src/lib.rs is empty. Its de-facto contract is the on-disk data it ships:
+ *   - scene JSON        scenes/cbox.json:1-628, scenes/room.json:1-3900
+ *   - integrator JSON   scenes/integrator.json:1-9
+ *   - BSON `.mesh`      scenes/*.mesh (name, vertices, normals, texcoords, indices)
+ * Each entry point below names the part of that contract (file:line) it serves.
+ * A Rust `extern "C"` crate binds these 1:1 (no torch types, plain pointers and
+ * sizes, no exceptions across the boundary).
+ *
+ * Threading: one aqua_ctx owns one CUDA device and one stream. Calls on the same
+ * context must be serialised by the caller; different contexts may be used from
+ * different threads.
+ */
+#ifndef AQUA_H
+#define AQUA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define AQUA_API __declspec(dllexport)
+#else
+#define AQUA_API __attribute__((visibility("default")))
+#endif
+
+/* ---------------------------------------------------------------- status */
+typedef enum aqua_status {
+    AQUA_OK = 0,
+    AQUA_ERR_INVALID_ARG = 1,   /* null handle, bad size, bad enum            */
+    AQUA_ERR_IO = 2,            /* file cannot be opened or read              */
+    AQUA_ERR_PARSE = 3,         /* malformed JSON / BSON / unknown enum tag   */
+    AQUA_ERR_MISSING_ASSET = 4, /* a referenced .mesh or texture is absent    */
+    AQUA_ERR_CUDA = 5,          /* a CUDA runtime call failed                 */
+    AQUA_ERR_OOM = 6,           /* host or device allocation failed           */
+    AQUA_ERR_TIMEOUT = 7,       /* a bounded device wait gave up              */
+    AQUA_ERR_UNSUPPORTED = 8    /* valid input this build does not implement  */
+} aqua_status;
+
+typedef struct aqua_ctx aqua_ctx;
+typedef struct aqua_scene aqua_scene;
+
+/* aqua_options.device value for a context without a GPU: scenes load, BVHs
+ * build and every export works; trace and render return AQUA_ERR_UNSUPPORTED. */
+#define AQUA_DEVICE_HOST_ONLY (-2)
+
+typedef struct aqua_options {
+    int32_t device;        /* CUDA ordinal; -1 = current device; AQUA_DEVICE_HOST_ONLY */
+    int32_t verbose;       /* 0 = silent                                         */
+    uint64_t fail_alloc_after; /* test hook: 0 = off; n = the n-th device
+                                  allocation of this context fails with OOM      */
+} aqua_options;
+
+/* One ray, 32 bytes: two 16-byte halves so the device reads it with two
+ * 128-bit loads. Directions need not be normalised; t is in units of |d|. */
+typedef struct aqua_ray {
+    float ox, oy, oz, tmin;
+    float dx, dy, dz, tmax;
+} aqua_ray;
+
+/* Closest hit, 16 bytes. prim = index of the triangle in scene order
+ * (the order of aqua_scene_export_triangles), -1 on a miss. The hit point is
+ * (1-u-v)*v0 + u*v1 + v*v2. For AQUA_TRACE_ANY_HIT, prim is 1 when occluded
+ * and -1 when not, and t/u/v are 0. */
+typedef struct aqua_hit {
+    float t, u, v;
+    int32_t prim;
+} aqua_hit;
+
+enum {
+    AQUA_TRACE_DEVICE_PTRS = 1u << 0, /* rays/hits are device pointers        */
+    AQUA_TRACE_ANY_HIT = 1u << 1,     /* occlusion query, early exit          */
+    AQUA_TRACE_COUNT = 1u << 2        /* fill aqua_trace_counts (slower)      */
+};
+
+/* Per-call traversal work, summed over all rays (node visits = internal nodes
+ * whose two child boxes were tested; tri tests = ray-triangle tests). */
+typedef struct aqua_trace_counts {
+    uint64_t node_visits;
+    uint64_t tri_tests;
+    double kernel_ms;     /* device time of the traversal kernel             */
+} aqua_trace_counts;
+
+/* Integrator settings. Mirrors scenes/integrator.json:1-9 (type, spp,
+ * batch_size, max_depth, training_iters, learning_rate, visualize_cache),
+ * plus the knobs the render path needs. */
+enum { AQUA_INTEGRATOR_PATH = 0, AQUA_INTEGRATOR_NRC = 1 };
+
+typedef struct aqua_integrator_cfg {
+    int32_t type;            /* AQUA_INTEGRATOR_PATH or AQUA_INTEGRATOR_NRC */
+    int32_t spp;             /* samples per pixel                           */
+    int32_t max_depth;       /* bounces; NEE at vertices 0..max_depth-1     */
+    int32_t rr_depth;        /* Russian roulette from this bounce on        */
+    int32_t batch_size;      /* NRC: training batch (integrator.json:4)     */
+    int32_t training_iters;  /* NRC: optimizer steps per frame              */
+    float learning_rate;     /* NRC: Adam step size (integrator.json:7)     */
+    int32_t visualize_cache; /* NRC: write the cache instead of radiance    */
+    uint64_t seed;           /* RNG seed: PCG32 stream per pixel            */
+    int32_t spp_offset;      /* first sample index (progressive rendering)  */
+    int32_t nrc_train_samples; /* NRC: training records per frame          */
+    int32_t nrc_query_vertex;  /* NRC: query the cache at this vertex       */
+    int32_t reserved0;
+} aqua_integrator_cfg;
+
+/* Launch shape of the wavefront. 0 in any field = the library default.
+ * Every choice gives a bit-identical image: each pixel is owned by exactly one
+ * path slot, which runs that pixel's samples in order. */
+typedef struct aqua_tuning {
+    int32_t slots;          /* paths in flight (0 = one per pixel, capped)   */
+    int32_t block_trace;    /* threads per block, traversal kernels          */
+    int32_t block_shade;    /* threads per block, shading kernel             */
+    int32_t sort_by_material; /* 1 = bin hits by material before shading     */
+    int32_t blocks_per_sm;  /* persistent grid = SMs * this                  */
+    int32_t use_graph;      /* 1 = replay iterations from a CUDA graph       */
+    int32_t iters_per_graph;/* iterations captured per graph                 */
+    int32_t reserved;
+} aqua_tuning;
+
+typedef struct aqua_stats {
+    uint64_t paths;          /* camera paths completed                       */
+    uint64_t ext_rays;       /* closest-hit rays traced                      */
+    uint64_t shadow_rays;    /* any-hit rays traced                          */
+    uint64_t iterations;     /* wavefront iterations                         */
+    double device_ms;        /* device time of the whole render              */
+    double trace_ms;         /* summed device time of closest-hit launches   */
+    double shadow_ms;        /* summed device time of any-hit launches       */
+    double shade_ms;         /* summed device time of shading launches       */
+    uint64_t trace_launches; /* closest-hit launches                         */
+    uint64_t shadow_launches;
+    uint64_t shade_launches;
+    uint64_t total_launches; /* every kernel this call launched              */
+    uint64_t node_visits;    /* filled when stage counting is requested      */
+    uint64_t tri_tests;
+    uint64_t shadow_node_visits;
+    uint64_t shadow_tri_tests;
+    uint64_t nrc_queries;    /* NRC: cache queries                           */
+    uint64_t nrc_train_records;
+    double nrc_ms;           /* NRC: device time of MLP kernels              */
+    double nrc_loss;         /* NRC: last training loss                      */
+} aqua_stats;
+
+enum {
+    AQUA_RENDER_DEVICE_FILM = 1u << 0, /* rgb_out is a device pointer         */
+    AQUA_RENDER_STAGE_TIMING = 1u << 1,/* fill the *_ms stage times          */
+    AQUA_RENDER_COUNT = 1u << 2,       /* fill node/tri counters (slower)    */
+    AQUA_RENDER_ACCUMULATE = 1u << 3   /* rgb_out += sum (no divide, no clear) */
+};
+
+/* Scene summary. */
+typedef struct aqua_scene_info {
+    int32_t width, height;
+    int32_t num_triangles, num_materials, num_lights, num_textures;
+    int32_t num_meshes, num_bvh_nodes;
+    int32_t bvh_depth, max_leaf_size;
+    uint64_t device_bytes;   /* device memory held by the scene             */
+    uint64_t upload_bytes;   /* bytes copied host->device by one upload     */
+    float env[3];            /* constant radiance seen by escaping rays     */
+    int32_t reserved;
+} aqua_scene_info;
+
+/* Camera, after parsing scenes/cbox.json:516-543 (`Perspective`). */
+typedef struct aqua_camera {
+    int32_t width, height;
+    float fov_deg;            /* full vertical field of view                */
+    float lens_radius, focal;
+    float pos[3];
+    float right[3], up[3], back[3]; /* camera looks along -back          */
+} aqua_camera;
+
+/* Material, the Lambert + GGX subset of `Principled` (scenes/cbox.json:3-62). */
+typedef struct aqua_material {
+    float base_color[3];      /* linear RGB (Srgb values are decoded)       */
+    int32_t base_texture;     /* -1 = none, else texture index              */
+    float metallic, roughness, specular;
+    int32_t reserved;
+} aqua_material;
+
+enum { AQUA_LIGHT_QUAD = 0, AQUA_LIGHT_POINT = 1, AQUA_LIGHT_TRIANGLE = 2 };
+
+typedef struct aqua_light {
+    int32_t type;
+    float p0[3], e1[3], e2[3]; /* quad: p0 + a*e1 + b*e2 (a, b in [0,1]);
+                                  triangle: the same with a + b <= 1;
+                                  both emit on the side of e1 x e2         */
+    float radiance[3];         /* quad: radiance; point: intensity          */
+    float pmf;                 /* selection probability (power-weighted)    */
+} aqua_light;
+
+/* A batched job: one view of one scene. */
+typedef struct aqua_job {
+    aqua_scene* scene;
+    int32_t width, height, spp, max_depth;
+    uint64_t seed;
+    float* rgb_out;           /* device pointer, width*height*3 floats      */
+} aqua_job;
+
+typedef struct aqua_batch_stats {
+    double device_ms;         /* whole batch, device time                   */
+    uint64_t paths;
+    double* job_ms;           /* optional, n entries: completion time of each
+                                 job measured from the start of the batch   */
+} aqua_batch_stats;
+
+/* ---------------------------------------------------------------- lifetime */
+AQUA_API aqua_status aqua_create(aqua_ctx** out, const aqua_options* opt);
+AQUA_API void aqua_destroy(aqua_ctx* ctx);
+/* Message of the last failing call on ctx ("" when none). Valid until the
+ * next call on ctx. aqua_create failures are reported by aqua_last_error(NULL). */
+AQUA_API const char* aqua_last_error(const aqua_ctx* ctx);
+AQUA_API const char* aqua_status_string(aqua_status s);
+AQUA_API int aqua_version(void);
+
+/* ---------------------------------------------------------------- scenes */
+/* Loads a scene JSON (scenes/cbox.json:1-628 schema: named_bsdfs, camera,
+ * lights, shapes) with its BSON meshes from the JSON's directory. A missing
+ * mesh (e.g. living_room_Default_43.mesh, .MISSING_LARGE_BLOBS:1) fails with
+ * AQUA_ERR_MISSING_ASSET unless allow_missing is set, which skips it. Image
+ * textures (room.json:6) need a JPEG decoder this build does not ship: they
+ * fail with AQUA_ERR_UNSUPPORTED unless allow_missing is set, which replaces
+ * them by the material's mid-grey. */
+AQUA_API aqua_status aqua_load_scene_json(aqua_ctx* ctx, const char* path,
+                                          int32_t allow_missing, aqua_scene** out);
+/* Procedural scenes 1..5: 1 = Cornell box (Lambert), 2 = Cornell box with GGX
+ * (roughness U[0.05,0.8], metallic {0,1}), 3 = synthetic interior (153 meshes,
+ * ~1.2M triangles, 8 textures 2048^2, 16 quad lights), 4 = scene 3 for the
+ * radiance cache, 5 = random-sphere field (~4M triangles).
+ * width/height <= 0 keep the scene's own resolution. */
+AQUA_API aqua_status aqua_make_procedural_scene(aqua_ctx* ctx, int32_t config_id,
+                                                uint64_t seed, int32_t width,
+                                                int32_t height, aqua_scene** out);
+AQUA_API aqua_status aqua_scene_free(aqua_ctx* ctx, aqua_scene* scene);
+AQUA_API aqua_status aqua_scene_set_resolution(aqua_ctx* ctx, aqua_scene* scene,
+                                               int32_t width, int32_t height);
+/* Re-copies the scene's device arrays from its pinned host copy (what a
+ * loader does after building); used to time uploads end to end. */
+AQUA_API aqua_status aqua_scene_upload(aqua_ctx* ctx, aqua_scene* scene);
+AQUA_API aqua_status aqua_scene_get_info(aqua_ctx* ctx, const aqua_scene* scene,
+                                         aqua_scene_info* out);
+
+/* Host copies of the scene, for checkers and tools. Triangles in scene order:
+ * verts = 9 floats per triangle, uvs = 6 floats per triangle, mat = material
+ * index per triangle, light = index of the light the triangle is part of or -1.
+ * Any output may be NULL. */
+AQUA_API aqua_status aqua_scene_export_triangles(aqua_ctx* ctx, const aqua_scene* scene,
+                                                 float* verts, float* uvs, int32_t* mat,
+                                                 int32_t* light);
+AQUA_API aqua_status aqua_scene_export_camera(aqua_ctx* ctx, const aqua_scene* scene,
+                                              aqua_camera* out);
+AQUA_API aqua_status aqua_scene_export_materials(aqua_ctx* ctx, const aqua_scene* scene,
+                                                 aqua_material* out);
+AQUA_API aqua_status aqua_scene_export_lights(aqua_ctx* ctx, const aqua_scene* scene,
+                                              aqua_light* out);
+/* Texture i as RGBA8, row-major, sRGB-encoded. Pass rgba = NULL to query the size. */
+AQUA_API aqua_status aqua_scene_export_texture(aqua_ctx* ctx, const aqua_scene* scene,
+                                               int32_t i, int32_t* width, int32_t* height,
+                                               uint8_t* rgba);
+/* The flattened BVH as the device holds it: nodes = 16 floats per node (four
+ * 16-byte words, layout in bvh.h), tri_order[k] = scene index of the k-th
+ * triangle in leaf order. */
+AQUA_API aqua_status aqua_scene_export_bvh(aqua_ctx* ctx, const aqua_scene* scene,
+                                           float* nodes, int32_t* tri_order);
+
+/* ---------------------------------------------------------------- integrator */
+/* Parses scenes/integrator.json:1-9. Unknown `type` strings fail with
+ * AQUA_ERR_PARSE. Fields absent from the file keep aqua_integrator_defaults. */
+AQUA_API aqua_status aqua_load_integrator_json(aqua_ctx* ctx, const char* path,
+                                               aqua_integrator_cfg* out);
+AQUA_API void aqua_integrator_defaults(aqua_integrator_cfg* out);
+AQUA_API void aqua_tuning_defaults(aqua_tuning* out);
+
+/* ---------------------------------------------------------------- the hot path */
+/* Traces n rays against the scene BVH (closest hit, or any hit with
+ * AQUA_TRACE_ANY_HIT). counts may be NULL. */
+AQUA_API aqua_status aqua_trace(aqua_ctx* ctx, aqua_scene* scene, const aqua_ray* rays,
+                                size_t n, aqua_hit* out, uint32_t flags,
+                                aqua_trace_counts* counts);
+
+/* Renders the scene: rgb_out receives width*height*3 floats, the mean of spp
+ * samples per pixel (linear radiance), row 0 at the top. tuning and stats may
+ * be NULL. */
+AQUA_API aqua_status aqua_render(aqua_ctx* ctx, aqua_scene* scene,
+                                 const aqua_integrator_cfg* cfg, const aqua_tuning* tuning,
+                                 float* rgb_out, uint32_t flags, aqua_stats* stats);
+
+/* Times short renders over a grid of launch shapes and returns the fastest. */
+AQUA_API aqua_status aqua_autotune(aqua_ctx* ctx, aqua_scene* scene,
+                                   const aqua_integrator_cfg* cfg, aqua_tuning* out);
+
+/* Renders n jobs (uneven resolutions and spp, several scenes) in one
+ * persistent launch. */
+AQUA_API aqua_status aqua_render_batch(aqua_ctx* ctx, const aqua_job* jobs, size_t n,
+                                       const aqua_tuning* tuning, aqua_batch_stats* stats);
+
+/* Device memory currently held by the context's render workspace. */
+AQUA_API uint64_t aqua_workspace_bytes(const aqua_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AQUA_H */

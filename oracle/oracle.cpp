@@ -1,0 +1,726 @@
+// oracle.cpp — CPU oracle (test infrastructure; see oracle.h). Parity
+// unpinned: the reference ships no implementation to compare against.
+//
+// Built with -ffp-contract=off so that every float expression rounds once
+// per operation, which the bit-exact traversal comparison relies on.
+#include "oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// ------------------------------------------------------------------ vectors
+template <class T>
+struct V3 {
+    T x, y, z;
+};
+template <class T> V3<T> operator+(V3<T> a, V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class T> V3<T> operator-(V3<T> a, V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class T> V3<T> operator-(V3<T> a) { return {-a.x, -a.y, -a.z}; }
+template <class T> V3<T> operator*(V3<T> a, V3<T> b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+template <class T> V3<T> operator*(V3<T> a, T s) { return {a.x * s, a.y * s, a.z * s}; }
+template <class T> T dot3(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class T> V3<T> cross3(V3<T> a, V3<T> b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <class T> T len3(V3<T> a) { return std::sqrt(dot3(a, a)); }
+template <class T> V3<T> unit(V3<T> a) { return a * (T(1) / std::sqrt(dot3(a, a))); }
+template <class T> T max3(V3<T> a) { return std::max(a.x, std::max(a.y, a.z)); }
+template <class T> T at(V3<T> a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+template <class T> T luminance(V3<T> c) { return T(0.2126) * c.x + T(0.7152) * c.y + T(0.0722) * c.z; }
+
+inline float mn(float a, float b) { return a < b ? a : b; }
+inline float mx(float a, float b) { return a > b ? a : b; }
+
+// ------------------------------------------------------------------ PCG32
+struct Pcg {
+    uint64_t state, inc;
+    uint32_t next() {
+        uint64_t old = state;
+        state = old * 6364136223846793005ULL + inc;
+        uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        uint32_t rot = (uint32_t)(old >> 59u);
+        return (xs >> rot) | (xs << ((0u - rot) & 31u));
+    }
+    void seed(uint64_t initstate, uint64_t initseq) {
+        state = 0;
+        inc = (initseq << 1u) | 1u;
+        next();
+        state += initstate;
+        next();
+    }
+    double uniform() { return (double)(next() >> 8) * (1.0 / 16777216.0); }
+};
+uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+// Sample `sample` of pixel `pixel`: PCG32 stream `pixel`, start derived
+// from (seed, sample).
+Pcg path_rng(uint64_t seed, uint32_t pixel, uint32_t sample) {
+    Pcg r;
+    r.seed(mix64(seed ^ (0xD1B54A32D192ED03ULL * ((uint64_t)sample + 1ULL))), (uint64_t)pixel);
+    return r;
+}
+
+// ------------------------------------------------------------------ scene view
+struct Tri {
+    V3<float> a, b, c;
+};
+Tri tri_at(const orc_scene* s, int32_t i) {
+    const float* v = s->verts + 9 * (size_t)i;
+    return {{v[0], v[1], v[2]}, {v[3], v[4], v[5]}, {v[6], v[7], v[8]}};
+}
+
+// ------------------------------------------------------------------ FP32 watertight
+struct ShearF {
+    V3<float> o;
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+ShearF shear_f(V3<float> o, V3<float> d) {
+    ShearF s;
+    s.o = o;
+    float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+    s.kz = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+    s.kx = (s.kz + 1) % 3;
+    s.ky = (s.kx + 1) % 3;
+    if (at(d, s.kz) < 0.0f) std::swap(s.kx, s.ky);
+    s.Sx = at(d, s.kx) / at(d, s.kz);
+    s.Sy = at(d, s.ky) / at(d, s.kz);
+    s.Sz = 1.0f / at(d, s.kz);
+    return s;
+}
+// Returns true and (t, u, v) when tmin < t < tmax.
+bool hit_f(const ShearF& s, const Tri& tr, float tmin, float tmax, float& t, float& u, float& v) {
+    V3<float> A = tr.a - s.o, B = tr.b - s.o, Cc = tr.c - s.o;
+    float Az_ = at(A, s.kz), Bz_ = at(B, s.kz), Cz_ = at(Cc, s.kz);
+    float Ax = at(A, s.kx) - s.Sx * Az_, Ay = at(A, s.ky) - s.Sy * Az_;
+    float Bx = at(B, s.kx) - s.Sx * Bz_, By = at(B, s.ky) - s.Sy * Bz_;
+    float Cx = at(Cc, s.kx) - s.Sx * Cz_, Cy = at(Cc, s.ky) - s.Sy * Cz_;
+    float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    float det = (U + V) + W;
+    if (det == 0.0f) return false;
+    float T = ((U * (s.Sz * Az_)) + (V * (s.Sz * Bz_))) + (W * (s.Sz * Cz_));
+    float r = 1.0f / det;
+    float tt = T * r;
+    if (!(tt > tmin && tt < tmax)) return false;
+    t = tt;
+    u = V * r;
+    v = W * r;
+    return true;
+}
+
+// ------------------------------------------------------------------ FP64 watertight
+bool hit_d(V3<double> o, V3<double> d, const Tri& tr, double tmin, double tmax, double& t, double& u, double& v) {
+    double ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+    int kz = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+    int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
+    if (at(d, kz) < 0.0) std::swap(kx, ky);
+    double Sx = at(d, kx) / at(d, kz), Sy = at(d, ky) / at(d, kz), Sz = 1.0 / at(d, kz);
+    V3<double> a{tr.a.x, tr.a.y, tr.a.z}, b{tr.b.x, tr.b.y, tr.b.z}, c{tr.c.x, tr.c.y, tr.c.z};
+    V3<double> A = a - o, B = b - o, Cc = c - o;
+    double Ax = at(A, kx) - Sx * at(A, kz), Ay = at(A, ky) - Sy * at(A, kz);
+    double Bx = at(B, kx) - Sx * at(B, kz), By = at(B, ky) - Sy * at(B, kz);
+    double Cx = at(Cc, kx) - Sx * at(Cc, kz), Cy = at(Cc, ky) - Sy * at(Cc, kz);
+    double U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+    if ((U < 0 || V < 0 || W < 0) && (U > 0 || V > 0 || W > 0)) return false;
+    double det = U + V + W;
+    if (det == 0.0) return false;
+    double T = U * Sz * at(A, kz) + V * Sz * at(B, kz) + W * Sz * at(Cc, kz);
+    double tt = T / det;
+    if (!(tt > tmin && tt < tmax)) return false;
+    t = tt;
+    u = V / det;
+    v = W / det;
+    return true;
+}
+
+// ------------------------------------------------------------------ BVH walk
+// Visits the flattened BVH exactly as the device kernels do; calls
+// leaf(first, count) for every leaf reached, box(tfar) returns the current
+// far limit. Templated on the box test.
+struct Node {
+    float w[16];
+};
+inline const float* node_at(const orc_scene* s, int32_t i) { return s->nodes + 16 * (size_t)i; }
+
+struct RayF {
+    V3<float> o, d, invd;
+    float tmin, tmax;
+};
+inline float inv_safe(float d) {
+    float ad = std::fabs(d);
+    float dd = ad < 1e-20f ? (d < 0.0f ? -1e-20f : 1e-20f) : d;
+    return 1.0f / dd;
+}
+inline float entry_f(const float* lo_hi_xy, float loz, float hiz, const RayF& r, float tlim) {
+    float tx0 = (lo_hi_xy[0] - r.o.x) * r.invd.x, tx1 = (lo_hi_xy[1] - r.o.x) * r.invd.x;
+    float ty0 = (lo_hi_xy[2] - r.o.y) * r.invd.y, ty1 = (lo_hi_xy[3] - r.o.y) * r.invd.y;
+    float tz0 = (loz - r.o.z) * r.invd.z, tz1 = (hiz - r.o.z) * r.invd.z;
+    float tn = mx(mx(mn(tx0, tx1), mn(ty0, ty1)), mx(mn(tz0, tz1), r.tmin));
+    float tf = mn(mn(mx(tx0, tx1), mx(ty0, ty1)), mn(mx(tz0, tz1), tlim));
+    tf = tf * 1.00000036f;
+    return tn <= tf ? tn : std::numeric_limits<float>::infinity();
+}
+
+struct HitF {
+    float t, u, v;
+    int32_t leaf_idx, id;
+    uint32_t nodes, tris;
+};
+HitF trace_f(const orc_scene* s, V3<float> o, V3<float> d, float tmin, float tmax, bool any) {
+    RayF r{o, d, {inv_safe(d.x), inv_safe(d.y), inv_safe(d.z)}, tmin, tmax};
+    ShearF sh = shear_f(o, d);
+    HitF h{tmax, 0, 0, -1, 0x7fffffff, 0, 0};
+    int32_t stack[64];
+    int sp = 0;
+    int32_t node = 0;
+    const float inf = std::numeric_limits<float>::infinity();
+    while (true) {
+        while (node >= 0) {
+            const float* w = node_at(s, node);
+            h.nodes++;
+            float t0 = entry_f(w + 0, w[8], w[9], r, h.t);
+            float t1 = entry_f(w + 4, w[10], w[11], r, h.t);
+            int32_t c0, c1;
+            memcpy(&c0, &w[12], 4);
+            memcpy(&c1, &w[13], 4);
+            bool h0 = t0 != inf, h1 = t1 != inf;
+            if (h0 && h1) {
+                if (t1 < t0) { stack[sp++] = c0; node = c1; }
+                else { stack[sp++] = c1; node = c0; }
+            } else if (h0) node = c0;
+            else if (h1) node = c1;
+            else {
+                if (sp == 0) return h;
+                node = stack[--sp];
+            }
+        }
+        int32_t code = ~node;
+        int32_t first = code >> 3, cnt = code & 7;
+        for (int k = 0; k < cnt; ++k) {
+            int32_t id = s->tri_order[first + k];
+            float t, u, v;
+            h.tris++;
+            if (hit_f(sh, tri_at(s, id), tmin, tmax, t, u, v)) {
+                if (any) { h.t = t; h.leaf_idx = first + k; h.id = id; return h; }
+                if (t < h.t || (t == h.t && id < h.id)) { h.t = t; h.u = u; h.v = v; h.leaf_idx = first + k; h.id = id; }
+            }
+        }
+        if (sp == 0) return h;
+        node = stack[--sp];
+    }
+}
+
+// FP64 walk of the same tree (boxes are float, exact in double).
+struct HitD {
+    double t, u, v;
+    int32_t id;
+};
+HitD trace_d(const orc_scene* s, V3<double> o, V3<double> d, double tmin, double tmax, bool any) {
+    V3<double> invd{1.0 / (std::fabs(d.x) < 1e-300 ? 1e-300 : d.x), 1.0 / (std::fabs(d.y) < 1e-300 ? 1e-300 : d.y),
+                    1.0 / (std::fabs(d.z) < 1e-300 ? 1e-300 : d.z)};
+    HitD h{tmax, 0, 0, -1};
+    int32_t stack[64];
+    int sp = 0;
+    int32_t node = 0;
+    auto entry = [&](double lx, double hx, double ly, double hy, double lz, double hz) {
+        double tx0 = (lx - o.x) * invd.x, tx1 = (hx - o.x) * invd.x;
+        double ty0 = (ly - o.y) * invd.y, ty1 = (hy - o.y) * invd.y;
+        double tz0 = (lz - o.z) * invd.z, tz1 = (hz - o.z) * invd.z;
+        double tn = std::max(std::max(std::min(tx0, tx1), std::min(ty0, ty1)), std::max(std::min(tz0, tz1), tmin));
+        double tf = std::min(std::min(std::max(tx0, tx1), std::max(ty0, ty1)), std::min(std::max(tz0, tz1), h.t));
+        tf *= 1.0 + 1e-12;
+        return tn <= tf ? tn : std::numeric_limits<double>::infinity();
+    };
+    const double inf = std::numeric_limits<double>::infinity();
+    while (true) {
+        while (node >= 0) {
+            const float* w = node_at(s, node);
+            double t0 = entry(w[0], w[1], w[2], w[3], w[8], w[9]);
+            double t1 = entry(w[4], w[5], w[6], w[7], w[10], w[11]);
+            int32_t c0, c1;
+            memcpy(&c0, &w[12], 4);
+            memcpy(&c1, &w[13], 4);
+            bool h0 = t0 != inf, h1 = t1 != inf;
+            if (h0 && h1) {
+                if (t1 < t0) { stack[sp++] = c0; node = c1; }
+                else { stack[sp++] = c1; node = c0; }
+            } else if (h0) node = c0;
+            else if (h1) node = c1;
+            else {
+                if (sp == 0) return h;
+                node = stack[--sp];
+            }
+        }
+        int32_t code = ~node;
+        int32_t first = code >> 3, cnt = code & 7;
+        for (int k = 0; k < cnt; ++k) {
+            int32_t id = s->tri_order[first + k];
+            double t, u, v;
+            if (hit_d(o, d, tri_at(s, id), tmin, tmax, t, u, v)) {
+                if (any) { h.t = t; h.id = id; return h; }
+                if (t < h.t || (t == h.t && id < h.id)) { h.t = t; h.u = u; h.v = v; h.id = id; }
+            }
+        }
+        if (sp == 0) return h;
+        node = stack[--sp];
+    }
+}
+
+template <class F>
+void parallel_for(int64_t n, int threads, F&& f) {
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    threads = (int)std::min<int64_t>(threads, std::max<int64_t>(n, 1));
+    std::atomic<int64_t> next{0};
+    const int64_t chunk = 64;
+    auto work = [&]() {
+        while (true) {
+            int64_t b = next.fetch_add(chunk);
+            if (b >= n) break;
+            int64_t e = std::min(n, b + chunk);
+            for (int64_t i = b; i < e; ++i) f(i);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int i = 1; i < threads; ++i) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+}
+
+// ------------------------------------------------------------------ BSDF
+// Lambert + GGX, same definitions as the device (see oracle.h).
+template <class T>
+struct Mat {
+    V3<T> color, F0;
+    T metallic, alpha, p_spec;
+    bool has_spec;
+};
+template <class T>
+Mat<T> make_mat(V3<T> color, T metallic, T roughness, T specular) {
+    Mat<T> m;
+    m.color = color;
+    m.metallic = metallic;
+    m.alpha = std::max(roughness * roughness, T(1e-3));
+    T f0d = T(0.08) * specular;
+    m.F0 = {f0d + (color.x - f0d) * metallic, f0d + (color.y - f0d) * metallic, f0d + (color.z - f0d) * metallic};
+    m.has_spec = (m.F0.x + m.F0.y + m.F0.z) > T(0);
+    T ws = luminance(m.F0), wd = (T(1) - metallic) * luminance(color);
+    T ps = (ws + wd) > T(0) ? ws / (ws + wd) : T(0.5);
+    if (ws > T(0) && wd > T(0)) ps = std::min(std::max(ps, T(0.1)), T(0.9));
+    if (!m.has_spec) ps = T(0);
+    m.p_spec = ps;
+    return m;
+}
+template <class T> T D_ggx(T a2, T c) {
+    T d = c * c * (a2 - T(1)) + T(1);
+    return a2 / (T(M_PI) * d * d);
+}
+template <class T> T Lambda(T a2, T c) {
+    T t2 = std::max(T(1) - c * c, T(0)) / (c * c);
+    return T(0.5) * (-T(1) + std::sqrt(T(1) + a2 * t2));
+}
+template <class T> V3<T> eval(const Mat<T>& m, V3<T> wo, V3<T> wi) {
+    if (wo.z <= T(0) || wi.z <= T(0)) return {0, 0, 0};
+    V3<T> f = m.color * ((T(1) - m.metallic) / T(M_PI));
+    if (!m.has_spec) return f;
+    V3<T> h = wo + wi;
+    T hl = len3(h);
+    if (hl > T(0)) {
+        h = h * (T(1) / hl);
+        T a2 = m.alpha * m.alpha;
+        T D = D_ggx(a2, h.z);
+        T G2 = T(1) / (T(1) + Lambda(a2, wo.z) + Lambda(a2, wi.z));
+        T c = std::min(std::max(T(1) - dot3(wi, h), T(0)), T(1));
+        T c5 = c * c * c * c * c;
+        V3<T> F{m.F0.x + (T(1) - m.F0.x) * c5, m.F0.y + (T(1) - m.F0.y) * c5, m.F0.z + (T(1) - m.F0.z) * c5};
+        f = f + F * (D * G2 / (T(4) * wo.z * wi.z));
+    }
+    return f;
+}
+template <class T> T pdf(const Mat<T>& m, V3<T> wo, V3<T> wi) {
+    if (wo.z <= T(0) || wi.z <= T(0)) return T(0);
+    T pd = wi.z / T(M_PI), ps = T(0);
+    if (m.p_spec > T(0)) {
+        V3<T> h = wo + wi;
+        T hl = len3(h);
+        if (hl > T(0)) {
+            h = h * (T(1) / hl);
+            T a2 = m.alpha * m.alpha;
+            ps = D_ggx(a2, h.z) / ((T(1) + Lambda(a2, wo.z)) * T(4) * wo.z);
+        }
+    }
+    return (T(1) - m.p_spec) * pd + m.p_spec * ps;
+}
+template <class T> V3<T> sample(const Mat<T>& m, V3<T> wo, T ul, T u1, T u2) {
+    if (ul < m.p_spec) {
+        T a = m.alpha;
+        V3<T> Vh = unit(V3<T>{a * wo.x, a * wo.y, wo.z});
+        T l2 = Vh.x * Vh.x + Vh.y * Vh.y;
+        V3<T> T1 = l2 > T(0) ? V3<T>{-Vh.y, Vh.x, T(0)} * (T(1) / std::sqrt(l2)) : V3<T>{1, 0, 0};
+        V3<T> T2 = cross3(Vh, T1);
+        T r = std::sqrt(u1), phi = T(2 * M_PI) * u2;
+        T t1 = r * std::cos(phi), t2 = r * std::sin(phi);
+        T s = T(0.5) * (T(1) + Vh.z);
+        t2 = (T(1) - s) * std::sqrt(std::max(T(1) - t1 * t1, T(0))) + s * t2;
+        V3<T> Nh = T1 * t1 + T2 * t2 + Vh * std::sqrt(std::max(T(0), T(1) - t1 * t1 - t2 * t2));
+        V3<T> Ne = unit(V3<T>{a * Nh.x, a * Nh.y, std::max(T(0), Nh.z)});
+        return Ne * (T(2) * dot3(wo, Ne)) - wo;
+    }
+    T r = std::sqrt(u1), phi = T(2 * M_PI) * u2;
+    return {r * std::cos(phi), r * std::sin(phi), std::sqrt(std::max(T(0), T(1) - u1))};
+}
+template <class T> T power(T a, T b) {
+    T a2 = a * a, b2 = b * b;
+    return (a2 + b2) > T(0) ? a2 / (a2 + b2) : T(0);
+}
+template <class T> void basis(V3<T> n, V3<T>& t, V3<T>& b) {
+    T sign = n.z >= T(0) ? T(1) : T(-1);
+    T a = T(-1) / (sign + n.z);
+    T bb = n.x * n.y * a;
+    t = {T(1) + sign * n.x * n.x * a, sign * bb, -sign * n.x};
+    b = {bb, sign + n.y * n.y * a, -n.y};
+}
+
+// Integer-ULP offset along the normal (Waechter & Binder, Ray Tracing Gems
+// 2019) for float; a relative epsilon for double.
+V3<float> offset(V3<float> p, V3<float> n) {
+    const float origin = 1.0f / 32.0f, fs = 1.0f / 65536.0f, is = 256.0f;
+    int32_t ix = (int32_t)(is * n.x), iy = (int32_t)(is * n.y), iz = (int32_t)(is * n.z);
+    auto bump = [](float x, int32_t d) {
+        int32_t b;
+        memcpy(&b, &x, 4);
+        b += x < 0 ? -d : d;
+        float r;
+        memcpy(&r, &b, 4);
+        return r;
+    };
+    return {std::fabs(p.x) < origin ? p.x + fs * n.x : bump(p.x, ix),
+            std::fabs(p.y) < origin ? p.y + fs * n.y : bump(p.y, iy),
+            std::fabs(p.z) < origin ? p.z + fs * n.z : bump(p.z, iz)};
+}
+V3<double> offset(V3<double> p, V3<double> n) {
+    double m = std::max(1.0, std::max(std::fabs(p.x), std::max(std::fabs(p.y), std::fabs(p.z))));
+    return p + n * (2e-6 * m);
+}
+
+// ------------------------------------------------------------------ integrator
+struct Lut {
+    double v[256];
+    Lut() {
+        for (int i = 0; i < 256; ++i) v[i] = orc_srgb_to_linear((double)i / 255.0);
+    }
+};
+
+template <class T>
+V3<T> texture(const orc_scene* s, const Lut& lut, int ti, T u, T v) {
+    int w = s->tex_w[ti], h = s->tex_h[ti];
+    const uint8_t* px = s->tex_rgba[ti];
+    T x = u * (T)w - T(0.5), y = v * (T)h - T(0.5);
+    T fx = std::floor(x), fy = std::floor(y);
+    T ax = x - fx, ay = y - fy;
+    long ix = (long)fx, iy = (long)fy;
+    auto tx = [&](long X, long Y) {
+        X %= w; if (X < 0) X += w;
+        Y %= h; if (Y < 0) Y += h;
+        const uint8_t* p = px + 4 * ((size_t)Y * (size_t)w + (size_t)X);
+        return V3<T>{(T)lut.v[p[0]], (T)lut.v[p[1]], (T)lut.v[p[2]]};
+    };
+    V3<T> c00 = tx(ix, iy), c10 = tx(ix + 1, iy), c01 = tx(ix, iy + 1), c11 = tx(ix + 1, iy + 1);
+    V3<T> a = c00 + (c10 - c00) * ax, b = c01 + (c11 - c01) * ax;
+    return a + (b - a) * ay;
+}
+
+struct Cam {
+    double tan_half, aspect;
+};
+
+template <class T>
+struct Closest {
+    bool hit;
+    T t, u, v;
+    int32_t id;
+};
+template <class T>
+Closest<T> closest(const orc_scene* s, V3<T> o, V3<T> d, T tmax, bool any);
+template <>
+Closest<float> closest<float>(const orc_scene* s, V3<float> o, V3<float> d, float tmax, bool any) {
+    HitF h = trace_f(s, o, d, 0.0f, tmax, any);
+    return {h.leaf_idx >= 0, h.t, h.u, h.v, h.id};
+}
+template <>
+Closest<double> closest<double>(const orc_scene* s, V3<double> o, V3<double> d, double tmax, bool any) {
+    HitD h = trace_d(s, o, d, 0.0, tmax, any);
+    return {h.id >= 0, h.t, h.u, h.v, h.id};
+}
+
+template <class T>
+void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>& cdf, int32_t spp, int32_t spp_offset,
+                  int32_t max_depth, int32_t rr_depth, uint64_t seed, uint32_t pixel, double sum[3], double st[3]) {
+    const aqua_camera& c = s->cam;
+    T tan_half = (T)std::tan(0.5 * (double)c.fov_deg * M_PI / 180.0);
+    T aspect = (T)c.width / (T)c.height;
+    V3<T> R{(T)c.right[0], (T)c.right[1], (T)c.right[2]}, U{(T)c.up[0], (T)c.up[1], (T)c.up[2]},
+        B{(T)c.back[0], (T)c.back[1], (T)c.back[2]}, P{(T)c.pos[0], (T)c.pos[1], (T)c.pos[2]};
+    V3<T> env{(T)s->env[0], (T)s->env[1], (T)s->env[2]};
+    const T inf = std::numeric_limits<T>::infinity();
+    uint32_t px = pixel % (uint32_t)c.width, py = pixel / (uint32_t)c.width;
+    for (int32_t si = 0; si < spp; ++si) {
+        Pcg rng = path_rng(seed, pixel, (uint32_t)(spp_offset + si));
+        T u0 = (T)rng.uniform(), u1 = (T)rng.uniform(), u2 = (T)rng.uniform(), u3 = (T)rng.uniform();
+        V3<T> dc{(T(2) * (((T)px + u0) / (T)c.width) - T(1)) * tan_half * aspect,
+                 (T(1) - T(2) * (((T)py + u1) / (T)c.height)) * tan_half, T(-1)};
+        V3<T> oc{0, 0, 0};
+        if (c.lens_radius > 0.0f) {
+            T a = T(2) * u2 - T(1), b = T(2) * u3 - T(1), lx = 0, ly = 0;
+            if (a != T(0) || b != T(0)) {
+                T r, phi;
+                if (std::fabs(a) > std::fabs(b)) { r = a; phi = T(M_PI / 4) * (b / a); }
+                else { r = b; phi = T(M_PI / 2) - T(M_PI / 4) * (a / b); }
+                lx = r * std::cos(phi);
+                ly = r * std::sin(phi);
+            }
+            oc = {lx * (T)c.lens_radius, ly * (T)c.lens_radius, T(0)};
+            dc = dc * (T)c.focal - oc;
+        }
+        V3<T> o = P + R * oc.x + U * oc.y + B * oc.z;
+        V3<T> d = unit(R * dc.x + U * dc.y + B * dc.z);
+        V3<T> thr{1, 1, 1};
+        T pdf_b = 0;
+        for (int depth = 0;; ++depth) {
+            st[1] += 1;
+            Closest<T> h = closest<T>(s, o, d, inf, false);
+            if (!h.hit) {
+                V3<T> e = thr * env;
+                sum[0] += e.x; sum[1] += e.y; sum[2] += e.z;
+                break;
+            }
+            const float* vv = s->verts + 9 * (size_t)h.id;
+            V3<T> v0{(T)vv[0], (T)vv[1], (T)vv[2]}, v1{(T)vv[3], (T)vv[4], (T)vv[5]}, v2{(T)vv[6], (T)vv[7], (T)vv[8]};
+            V3<T> e1 = v1 - v0, e2 = v2 - v0;
+            V3<T> p = v0 + e1 * h.u + e2 * h.v;
+            V3<T> ng = unit(cross3(e1, e2));
+            V3<T> wo = -d;
+            int light = s->tri_light[h.id];
+            if (light >= 0) {
+                const aqua_light& L = s->lights[light];
+                V3<T> le1{(T)L.e1[0], (T)L.e1[1], (T)L.e1[2]}, le2{(T)L.e2[0], (T)L.e2[1], (T)L.e2[2]};
+                V3<T> nl = unit(cross3(le1, le2));
+                T area = len3(cross3(le1, le2)) * (L.type == AQUA_LIGHT_TRIANGLE ? T(0.5) : T(1));
+                T cl = dot3(nl, wo);
+                if (cl > T(0)) {
+                    T w = 1;
+                    if (depth > 0 && pdf_b > T(0)) w = power(pdf_b, (T)L.pmf * h.t * h.t / (area * cl));
+                    V3<T> e = thr * V3<T>{(T)L.radiance[0], (T)L.radiance[1], (T)L.radiance[2]} * w;
+                    sum[0] += e.x; sum[1] += e.y; sum[2] += e.z;
+                }
+            }
+            if (depth >= max_depth) break;
+            if (dot3(ng, wo) < T(0)) ng = -ng;
+            const aqua_material& m = s->mats[s->tri_mat[h.id]];
+            V3<T> base{(T)m.base_color[0], (T)m.base_color[1], (T)m.base_color[2]};
+            if (m.base_texture >= 0) {
+                const float* uv = s->uvs + 6 * (size_t)h.id;
+                T w0 = T(1) - h.u - h.v;
+                T tu = (T)uv[0] * w0 + (T)uv[2] * h.u + (T)uv[4] * h.v;
+                T tv = (T)uv[1] * w0 + (T)uv[3] * h.u + (T)uv[5] * h.v;
+                base = base * texture<T>(s, lut, m.base_texture, tu, tv);
+            }
+            Mat<T> M = make_mat<T>(base, (T)m.metallic, (T)m.roughness, (T)m.specular);
+            V3<T> Tt, Bt;
+            basis(ng, Tt, Bt);
+            V3<T> wol{dot3(wo, Tt), dot3(wo, Bt), dot3(wo, ng)};
+            T u[8];
+            for (int k = 0; k < 8; ++k) u[k] = (T)rng.uniform();
+            if (s->n_lights > 0 && wol.z > T(0)) {
+                int li = 0;
+                while (li < s->n_lights - 1 && !((double)u[0] < cdf[(size_t)li])) ++li;
+                const aqua_light& L = s->lights[li];
+                V3<T> lp{(T)L.p0[0], (T)L.p0[1], (T)L.p0[2]};
+                V3<T> le{(T)L.radiance[0], (T)L.radiance[1], (T)L.radiance[2]};
+                T pmf = (T)L.pmf;
+                V3<T> contrib{0, 0, 0}, wi{0, 0, 1};
+                T dist = 0;
+                if (L.type == AQUA_LIGHT_POINT) {
+                    V3<T> dl = lp - p;
+                    T d2 = dot3(dl, dl);
+                    dist = std::sqrt(d2);
+                    wi = dl * (T(1) / dist);
+                    T cs = dot3(wi, ng);
+                    if (cs > T(0) && d2 > T(0)) {
+                        V3<T> wil{dot3(wi, Tt), dot3(wi, Bt), cs};
+                        contrib = thr * eval(M, wol, wil) * le * (cs / (d2 * pmf));
+                    }
+                } else {
+                    V3<T> le1{(T)L.e1[0], (T)L.e1[1], (T)L.e1[2]}, le2{(T)L.e2[0], (T)L.e2[1], (T)L.e2[2]}, xl;
+                    if (L.type == AQUA_LIGHT_QUAD) xl = lp + le1 * u[1] + le2 * u[2];
+                    else {
+                        T su = std::sqrt(u[1]);
+                        xl = lp + le1 * (su * (T(1) - u[2])) + le2 * (su * u[2]);
+                    }
+                    V3<T> cr = cross3(le1, le2);
+                    V3<T> nl = unit(cr);
+                    T area = len3(cr) * (L.type == AQUA_LIGHT_TRIANGLE ? T(0.5) : T(1));
+                    V3<T> dl = xl - p;
+                    T d2 = dot3(dl, dl);
+                    dist = std::sqrt(d2);
+                    wi = dl * (T(1) / dist);
+                    T cl = -dot3(wi, nl), cs = dot3(wi, ng);
+                    if (cl > T(0) && cs > T(0) && d2 > T(0)) {
+                        V3<T> wil{dot3(wi, Tt), dot3(wi, Bt), cs};
+                        T pl = pmf * d2 / (area * cl);
+                        T w = power(pl, pdf(M, wol, wil));
+                        contrib = thr * eval(M, wol, wil) * le * (cs * w / pl);
+                    }
+                }
+                if (contrib.x > T(0) || contrib.y > T(0) || contrib.z > T(0)) {
+                    st[2] += 1;
+                    Closest<T> o2 = closest<T>(s, offset(p, ng), wi, dist * T(1.0 - 1e-4), true);
+                    if (!o2.hit) { sum[0] += contrib.x; sum[1] += contrib.y; sum[2] += contrib.z; }
+                }
+            }
+            V3<T> wil = sample(M, wol, u[3], u[4], u[5]);
+            if (!(wil.z > T(0) && wol.z > T(0))) break;
+            T pb = pdf(M, wol, wil);
+            if (!(pb > T(0))) break;
+            thr = thr * eval(M, wol, wil) * (wil.z / pb);
+            if (!(max3(thr) > T(0)) || !std::isfinite(thr.x) || !std::isfinite(thr.y) || !std::isfinite(thr.z)) break;
+            if (depth >= rr_depth) {
+                T q = std::min(T(1), max3(thr));
+                if (u[6] >= q) break;
+                thr = thr * (T(1) / q);
+            }
+            d = unit(Tt * wil.x + Bt * wil.y + ng * wil.z);
+            o = offset(p, ng);
+            pdf_b = pb;
+        }
+        st[0] += 1;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+double orc_srgb_to_linear(double c) { return c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4); }
+
+uint32_t orc_pcg32_first(uint64_t initstate, uint64_t initseq, uint32_t* out, int n) {
+    Pcg r;
+    r.seed(initstate, initseq);
+    uint32_t last = 0;
+    for (int i = 0; i < n; ++i) {
+        last = r.next();
+        if (out) out[i] = last;
+    }
+    return last;
+}
+
+void orc_trace_bvh_f32(const orc_scene* s, const float* rays, int64_t n, int any_hit, float* hits,
+                       uint32_t* counts, int threads) {
+    parallel_for(n, threads, [&](int64_t i) {
+        const float* r = rays + 8 * i;
+        HitF h = trace_f(s, {r[0], r[1], r[2]}, {r[4], r[5], r[6]}, r[3], r[7], any_hit != 0);
+        float* o = hits + 4 * i;
+        int32_t prim = h.leaf_idx >= 0 ? (any_hit ? 1 : h.id) : -1;
+        if (any_hit || h.leaf_idx < 0) { o[0] = o[1] = o[2] = 0.0f; }
+        else { o[0] = h.t; o[1] = h.u; o[2] = h.v; }
+        memcpy(&o[3], &prim, 4);
+        if (counts) { counts[2 * i] = h.nodes; counts[2 * i + 1] = h.tris; }
+    });
+}
+
+void orc_trace_brute_f32(const orc_scene* s, const float* rays, int64_t n, int any_hit, float* hits, int threads) {
+    parallel_for(n, threads, [&](int64_t i) {
+        const float* r = rays + 8 * i;
+        V3<float> o{r[0], r[1], r[2]}, d{r[4], r[5], r[6]};
+        ShearF sh = shear_f(o, d);
+        float bt = r[7], bu = 0, bv = 0;
+        int32_t bid = -1;
+        for (int32_t k = 0; k < s->n_tris; ++k) {
+            float t, u, v;
+            if (hit_f(sh, tri_at(s, k), r[3], r[7], t, u, v)) {
+                if (bid < 0 || t < bt || (t == bt && k < bid)) { bt = t; bu = u; bv = v; bid = k; }
+                if (any_hit) break;
+            }
+        }
+        float* out = hits + 4 * i;
+        int32_t prim = bid >= 0 ? (any_hit ? 1 : bid) : -1;
+        if (any_hit || bid < 0) { out[0] = out[1] = out[2] = 0.0f; }
+        else { out[0] = bt; out[1] = bu; out[2] = bv; }
+        memcpy(&out[3], &prim, 4);
+    });
+}
+
+void orc_trace_brute_f64(const orc_scene* s, const float* rays, int64_t n, double* hits, int threads) {
+    parallel_for(n, threads, [&](int64_t i) {
+        const float* r = rays + 8 * i;
+        V3<double> o{r[0], r[1], r[2]}, d{r[4], r[5], r[6]};
+        double bt = r[7], bu = 0, bv = 0;
+        int32_t bid = -1;
+        for (int32_t k = 0; k < s->n_tris; ++k) {
+            double t, u, v;
+            if (hit_d(o, d, tri_at(s, k), (double)r[3], (double)r[7], t, u, v)) {
+                if (bid < 0 || t < bt || (t == bt && k < bid)) { bt = t; bu = u; bv = v; bid = k; }
+            }
+        }
+        double* out = hits + 4 * i;
+        out[0] = bid >= 0 ? bt : 0.0;
+        out[1] = bu;
+        out[2] = bv;
+        out[3] = (double)bid;
+    });
+}
+
+int orc_render(const orc_scene* s, int precision, int32_t spp, int32_t spp_offset, int32_t max_depth,
+               int32_t rr_depth, uint64_t seed, int threads, int64_t pixel_begin, int64_t pixel_end, float* out,
+               double* stats) {
+    if (!s || !out || spp <= 0 || (precision != 32 && precision != 64)) return 1;
+    int64_t npix = (int64_t)s->cam.width * s->cam.height;
+    pixel_begin = std::max<int64_t>(0, pixel_begin);
+    pixel_end = std::min<int64_t>(npix, pixel_end);
+    if (pixel_end <= pixel_begin) return 0;
+    static const Lut lut;
+    std::vector<double> cdf((size_t)std::max(s->n_lights, 1));
+    // Light-selection CDF: running double sum of the float pmfs, stored as
+    // float, last entry 1 (the table the device searches).
+    double acc = 0;
+    for (int i = 0; i < s->n_lights; ++i) {
+        acc += (double)s->lights[i].pmf;
+        cdf[(size_t)i] = (i + 1 == s->n_lights) ? 1.0 : (double)(float)acc;
+    }
+    int64_t n = pixel_end - pixel_begin;
+    std::vector<double> st((size_t)n * 3, 0.0);
+    parallel_for(n, threads, [&](int64_t k) {
+        uint32_t pixel = (uint32_t)(pixel_begin + k);
+        double sum[3] = {0, 0, 0};
+        double* sk = &st[3 * (size_t)k];
+        if (precision == 64)
+            render_pixel<double>(s, lut, cdf, spp, spp_offset, max_depth, rr_depth, seed, pixel, sum, sk);
+        else
+            render_pixel<float>(s, lut, cdf, spp, spp_offset, max_depth, rr_depth, seed, pixel, sum, sk);
+        for (int c = 0; c < 3; ++c) out[3 * (size_t)pixel + c] = (float)(sum[c] / spp);
+    });
+    if (stats) {
+        stats[0] = stats[1] = stats[2] = 0;
+        for (int64_t k = 0; k < n; ++k)
+            for (int c = 0; c < 3; ++c) stats[c] += st[3 * (size_t)k + c];
+    }
+    return 0;
+}
+
+}  // extern "C"

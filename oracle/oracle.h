@@ -1,0 +1,81 @@
+/*
+ * oracle.h — CPU oracle for the light-transport hot path. TEST
+ * INFRASTRUCTURE ONLY: the tests, the smoke check and the benchmark's CPU
+ * baseline call it as the checker; the library never links or calls it.
+ *
+ * Parity is unpinned: the reference (`arukas`, src/lib.rs) ships no
+ * implementation, no tests and no golden images, so nothing here is checked
+ * against reference outputs. What is pinned are the reference's data facts
+ * (tests/golden/reference_facts.json) and published algorithms:
+ *   - watertight ray/triangle test, Woop, Benthin, Wald, JCGT 2(1) 2013
+ *   - robust slab test, Ize, JCGT 2(2) 2013
+ *   - GGX / Smith (Walter et al. EGSR 2007), VNDF (Heitz JCGT 7(4) 2018),
+ *     Schlick Fresnel, power-heuristic MIS (Veach 1997)
+ *   - PCG32 (O'Neill 2014), SplitMix64 (Steele et al. 2014)
+ * Scene semantics follow scenes/cbox.json:1-628 (camera 516-543, Principled
+ * 3-62, Point lights 544-561), CornellBox-Original.mtl:80-87 (quad light) and
+ * scenes/integrator.json:5 (max_depth).
+ *
+ * Scene layout structures (aqua_material, aqua_light, aqua_camera) come from
+ * include/aqua.h, the data contract both sides read.
+ */
+#ifndef AQUA_ORACLE_H
+#define AQUA_ORACLE_H
+
+#include <stdint.h>
+
+#include "../include/aqua.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_scene {
+    const float* nodes;        /* flattened BVH, 16 floats per node     */
+    int32_t n_nodes;
+    const int32_t* tri_order;  /* leaf order -> scene triangle          */
+    const float* verts;        /* 9 floats per triangle, scene order    */
+    const float* uvs;          /* 6 floats per triangle                 */
+    const int32_t* tri_mat;
+    const int32_t* tri_light;
+    int32_t n_tris;
+    const aqua_material* mats;
+    int32_t n_mats;
+    const aqua_light* lights;
+    int32_t n_lights;
+    const uint8_t* const* tex_rgba; /* n_tex pointers, sRGB RGBA8    */
+    const int32_t* tex_w;
+    const int32_t* tex_h;
+    int32_t n_tex;
+    aqua_camera cam;
+    float env[3];
+} orc_scene;
+
+/* FP32 traversal of the flattened BVH with the same node order, slab test
+ * and triangle arithmetic as the device kernels. rays: 8 floats per ray;
+ * hits: 4 floats (t, u, v, prim bits) per ray; counts: per-ray node visits
+ * and triangle tests (2 uint32 per ray), may be NULL. */
+void orc_trace_bvh_f32(const orc_scene* s, const float* rays, int64_t n, int any_hit, float* hits,
+                       uint32_t* counts, int threads);
+/* FP32 watertight test against every triangle; min (t, prim). */
+void orc_trace_brute_f32(const orc_scene* s, const float* rays, int64_t n, int any_hit, float* hits, int threads);
+/* FP64 watertight test against every triangle; hits: 4 doubles per ray. */
+void orc_trace_brute_f64(const orc_scene* s, const float* rays, int64_t n, double* hits, int threads);
+
+/* Path tracer with the device's estimator and random-number use, in
+ * double (precision 64) or float (precision 32). Renders pixels
+ * [pixel_begin, pixel_end) into out (width*height*3 floats, mean of spp).
+ * stats: [paths, extension rays, shadow rays]. Returns 0 on success. */
+int orc_render(const orc_scene* s, int precision, int32_t spp, int32_t spp_offset, int32_t max_depth,
+               int32_t rr_depth, uint64_t seed, int threads, int64_t pixel_begin, int64_t pixel_end,
+               float* out, double* stats);
+
+/* Reference values the tests print. */
+double orc_srgb_to_linear(double c);
+uint32_t orc_pcg32_first(uint64_t initstate, uint64_t initseq, uint32_t* out, int n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,131 @@
+"""Image parity on the GPU: the wavefront renderer against the FP64 oracle.
+
+relMSE = mean over pixels and channels of (x - r)^2 / (r^2 + 1e-2).
+Sample-matched tests use the same seed on both sides (same PCG32 stream per
+pixel, same random numbers per bounce), so the images agree far below the
+1e-3 bar; the converged test uses independent seeds and high spp.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-3  # relMSE bar against the FP64 oracle
+
+
+def rel_mse(x, r):
+    import pyoracle
+
+    return pyoracle.rel_mse(x, r)
+
+
+@pytest.mark.parametrize("config,depth", [(1, 5), (2, 8)])
+def test_cornell_sample_matched(gpu_ctx, config, depth):
+    import pyoracle
+
+    s = gpu_ctx.procedural(config, seed=0, width=48, height=48)
+    o = pyoracle.OracleScene.from_aqua(s)
+    cfg = gpu_ctx.integrator(spp=128, max_depth=depth, rr_depth=3, seed=11)
+    img, st = gpu_ctx.render(s, cfg)
+    ref, ost = o.render(128, depth, seed=11, precision=64)
+    err = rel_mse(img, ref)
+    assert err < TOL, err
+    assert st.paths == 48 * 48 * 128 == int(ost[0])
+    # Same random numbers: ray counts agree to within rare FP32/FP64 divergences.
+    assert abs(st.ext_rays - ost[1]) / ost[1] < 2e-3
+    assert abs(st.shadow_rays - ost[2]) / ost[2] < 2e-3
+    s.free()
+
+
+def test_cornell_converged_independent_seeds(gpu_ctx):
+    import pyoracle
+
+    s = gpu_ctx.procedural(2, seed=0, width=24, height=24)
+    o = pyoracle.OracleScene.from_aqua(s)
+    cfg = gpu_ctx.integrator(spp=16384, max_depth=8, rr_depth=3, seed=101)
+    img, _ = gpu_ctx.render(s, cfg)
+    ref, _ = o.render(16384, 8, seed=202, precision=64)
+    err = rel_mse(img, ref)
+    assert err < TOL, err
+    s.free()
+
+
+def test_interior_textured_sample_matched(gpu_ctx):
+    import pyoracle
+
+    s = gpu_ctx.procedural(3, seed=0, width=64, height=36)
+    o = pyoracle.OracleScene.from_aqua(s)
+    cfg = gpu_ctx.integrator(spp=16, max_depth=8, rr_depth=3, seed=3)
+    img, st = gpu_ctx.render(s, cfg)
+    ref, _ = o.render(16, 8, seed=3, precision=64)
+    err = rel_mse(img, ref)
+    assert err < TOL, err
+    assert img.mean() > 0.01
+    s.free()
+
+
+def test_launch_shape_does_not_change_the_image(gpu_ctx):
+    s = gpu_ctx.procedural(2, seed=0, width=40, height=30)
+    cfg = gpu_ctx.integrator(spp=32, max_depth=8, rr_depth=3, seed=9)
+    base, _ = gpu_ctx.render(s, cfg)
+    for kw in [dict(slots=1000), dict(slots=37), dict(sort_by_material=1), dict(block_trace=64, block_shade=32),
+               dict(slots=333, sort_by_material=1, blocks_per_sm=2)]:
+        img, _ = gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning(**kw))
+        assert np.array_equal(img.view(np.uint32), base.view(np.uint32)), kw
+    s.free()
+
+
+def test_depth_zero_sees_only_emitters(gpu_ctx):
+    import pyoracle
+
+    s = gpu_ctx.procedural(1, seed=0, width=64, height=64)
+    cfg = gpu_ctx.integrator(spp=4, max_depth=0, rr_depth=3, seed=1)
+    img, st = gpu_ctx.render(s, cfg)
+    assert st.shadow_rays == 0
+    lit = img.max(axis=2) > 0
+    assert 0 < lit.mean() < 0.05  # only the ceiling light is visible
+    o = pyoracle.OracleScene.from_aqua(s)
+    ref, _ = o.render(4, 0, seed=1, precision=64)
+    assert rel_mse(img, ref) < TOL
+    s.free()
+
+
+def test_progressive_accumulation_matches_one_call(gpu_ctx):
+    import aqua
+
+    s = gpu_ctx.procedural(2, seed=0, width=32, height=32)
+    full, _ = gpu_ctx.render(s, gpu_ctx.integrator(spp=16, max_depth=8, seed=4))
+    acc = np.zeros_like(full)
+    for off in range(0, 16, 4):
+        gpu_ctx.render(s, gpu_ctx.integrator(spp=4, max_depth=8, seed=4, spp_offset=off), out=acc,
+                       flags=aqua.RENDER_ACCUMULATE)
+    np.testing.assert_allclose(acc / 16, full, rtol=1e-5, atol=1e-6)
+    s.free()
+
+
+def test_invalid_arguments_raise(gpu_ctx):
+    import aqua
+
+    s = gpu_ctx.procedural(1, seed=0, width=8, height=8)
+    with pytest.raises(aqua.AquaError) as e:
+        gpu_ctx.render(s, gpu_ctx.integrator(spp=0))
+    assert e.value.status == aqua.ERR_INVALID_ARG
+    with pytest.raises(aqua.AquaError) as e:
+        gpu_ctx.render(s, gpu_ctx.integrator(spp=1), tuning=gpu_ctx.tuning(block_trace=100))
+    assert e.value.status == aqua.ERR_INVALID_ARG
+    s.free()
+
+
+def test_stats_and_stage_timing(gpu_ctx):
+    import aqua
+
+    s = gpu_ctx.procedural(2, seed=0, width=64, height=64)
+    img, st = gpu_ctx.render(s, gpu_ctx.integrator(spp=8, max_depth=8, seed=2),
+                             flags=aqua.RENDER_STAGE_TIMING | aqua.RENDER_COUNT)
+    assert st.paths == 64 * 64 * 8
+    assert st.trace_ms > 0 and st.shade_ms > 0 and st.shadow_ms > 0
+    assert st.device_ms >= st.trace_ms
+    assert st.node_visits > st.ext_rays and st.tri_tests > 0
+    s.free()
