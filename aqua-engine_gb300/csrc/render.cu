@@ -423,6 +423,8 @@ __global__ void k_resolve(const float4* film, float* out, uint32_t pixels, float
 // ---------------------------------------------------------------- host side
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+constexpr uint64_t kStageTimingStride = 8;
+
 static void ensure_workspace(aqua_ctx* ctx, size_t slots, size_t buckets, size_t pixels) {
     Workspace& w = ctx->ws;
     if (w.block.ptr && w.slots >= slots && w.buckets >= buckets && w.pixels >= pixels) return;
@@ -584,15 +586,16 @@ void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, 
             uint32_t in = (uint32_t)(iter & 1), out = 1u - in;
             W.q_in = w.q[in];
             W.q_out = w.q[out];
-            tt.begin();
+            // Stage timing brackets every kStageTimingStride-th iteration so
+            // the events barely perturb the launch stream.
+            bool timed = timing && (iter % kStageTimingStride) == 0;
+            if (timed) tt.begin();
             trace_k<<<g_trace, bt, 0, st>>>(S, P, W, in, out);
-            tt.end();
-            ts.begin();
+            if (timed) { tt.end(); ts.begin(); }
             shade_k<<<g_shade, bs, 0, st>>>(S, P, W, in, out);
-            ts.end();
-            tsh.begin();
+            if (timed) { ts.end(); tsh.begin(); }
             shadow_k<<<g_shadow, bt, 0, st>>>(S, P, W);
-            tsh.end();
+            if (timed) tsh.end();
             launches += 3;
         }
         AQ_CUDA(cudaGetLastError());
@@ -635,9 +638,10 @@ void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, 
         stats->ext_rays = hs[kStatExt];
         stats->shadow_rays = hs[kStatShadow];
         stats->iterations = iter;
-        stats->trace_launches = iter;
-        stats->shade_launches = iter;
-        stats->shadow_launches = iter;
+        // With stage timing: the launches whose times the *_ms fields sum.
+        stats->trace_launches = timing ? tt.pairs.size() : iter;
+        stats->shade_launches = timing ? ts.pairs.size() : iter;
+        stats->shadow_launches = timing ? tsh.pairs.size() : iter;
         stats->total_launches = launches;
         stats->node_visits = hs[kStatNodes];
         stats->tri_tests = hs[kStatTris];

@@ -226,7 +226,9 @@ def run_gpu(args, world, rank, local, pg):
         for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
+            torch.cuda.nvtx.range_push("timed_step")
             steps.append(ctx.render_device(scene, cfg, film.data_ptr(), tune, flags=aqua.RENDER_STAGE_TIMING))
+            torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     barrier(pg)
@@ -304,7 +306,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic-per-launch", type=float, default=None,
                     help="DRAM bytes per k_trace_ext launch from an ncu capture")
+    ap.add_argument("--spp", type=int, default=0,
+                    help="samples per pixel of the workload (default 1024; smaller only for profiling captures)")
     args = ap.parse_args()
+    if args.spp > 0 and args.spp != WORKLOAD["spp"]:
+        WORKLOAD["spp"] = args.spp
+        WORKLOAD["workload"] = f"cornell-ggx-1024x1024-{args.spp}spp-depth8"
     if args.warmup < 3:
         log("warning: fewer than 3 warm-up steps")
     world, rank, local, pg = dist_setup(args.gpus)

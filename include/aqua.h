@@ -128,10 +128,13 @@ typedef struct aqua_stats {
     uint64_t shadow_rays;    /* any-hit rays traced                          */
     uint64_t iterations;     /* wavefront iterations                         */
     double device_ms;        /* device time of the whole render              */
-    double trace_ms;         /* summed device time of closest-hit launches   */
-    double shadow_ms;        /* summed device time of any-hit launches       */
-    double shade_ms;         /* summed device time of shading launches       */
-    uint64_t trace_launches; /* closest-hit launches                         */
+    /* With AQUA_RENDER_STAGE_TIMING, every 8th wavefront iteration has its
+     * three launches bracketed by CUDA events; *_ms sum those launches and
+     * *_launches count them. Without it, *_launches count every launch. */
+    double trace_ms;         /* closest-hit (extension ray) launches         */
+    double shadow_ms;        /* any-hit (shadow ray) launches                */
+    double shade_ms;         /* shading launches                             */
+    uint64_t trace_launches;
     uint64_t shadow_launches;
     uint64_t shade_launches;
     uint64_t total_launches; /* every kernel this call launched              */

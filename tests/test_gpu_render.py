@@ -129,3 +129,20 @@ def test_stats_and_stage_timing(gpu_ctx):
     assert st.device_ms >= st.trace_ms
     assert st.node_visits > st.ext_rays and st.tri_tests > 0
     s.free()
+
+
+def test_allocation_failure_is_reported():
+    import aqua
+
+    # The first device allocation of this context (the scene image) fails.
+    with aqua.Context(device=0, fail_alloc_after=1) as c:
+        with pytest.raises(aqua.AquaError) as e:
+            c.procedural(1, seed=0, width=8, height=8)
+        assert e.value.status == aqua.ERR_OOM and "fail_alloc_after" in e.value.message
+    # The second one (the render workspace) fails; the context stays usable.
+    with aqua.Context(device=0, fail_alloc_after=2) as c:
+        s = c.procedural(1, seed=0, width=8, height=8)
+        with pytest.raises(aqua.AquaError) as e:
+            c.render(s, c.integrator(spp=1))
+        assert e.value.status == aqua.ERR_OOM
+        s.free()
