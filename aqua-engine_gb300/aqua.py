@@ -151,6 +151,8 @@ SIGNATURES = [
     ("aqua_autotune", C.c_int, [_P, _P, C.POINTER(IntegratorCfg), C.POINTER(Tuning)]),
     ("aqua_render_batch", C.c_int, [_P, _P, C.c_size_t, C.POINTER(Tuning), C.POINTER(BatchStats)]),
     ("aqua_workspace_bytes", C.c_uint64, [_P]),
+    ("aqua_render_noalloc", C.c_int, [_P, _P, C.POINTER(IntegratorCfg), _P, C.POINTER(Stats)]),
+    ("aqua_render_noalloc_max_pixels", C.c_uint64, []),
 ]
 
 _lib = None

@@ -505,4 +505,17 @@ AQUA_API aqua_status aqua_render_batch(aqua_ctx* ctx, const aqua_job* jobs, size
 
 AQUA_API uint64_t aqua_workspace_bytes(const aqua_ctx* ctx) { return ctx ? ctx->ws.block.bytes : 0; }
 
+AQUA_API aqua_status aqua_render_noalloc(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg* cfg,
+                                         float* rgb_out_device, aqua_stats* stats) {
+    return guard(ctx, [&]() {
+        need(s && cfg && rgb_out_device, "scene, cfg and rgb_out_device must be non-NULL");
+        need_device(ctx);
+        if (cfg->type != AQUA_INTEGRATOR_PATH)
+            throw Error(AQUA_ERR_UNSUPPORTED, "aqua_render_noalloc renders the path integrator only");
+        render_noalloc(ctx, s, *cfg, rgb_out_device, stats);
+    });
+}
+
+AQUA_API uint64_t aqua_render_noalloc_max_pixels(void) { return (uint64_t)render_noalloc_max_pixels(); }
+
 }  // extern "C"

@@ -109,4 +109,9 @@ void render_path(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg& cfg, c
                  float* rgb_out, uint32_t flags, aqua_stats* stats);
 void workspace_release(aqua_ctx* ctx);
 
+// Render on the library's fixed static scratch array; no device allocation.
+void render_noalloc(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg& cfg, float* rgb_out,
+                    aqua_stats* stats);
+size_t render_noalloc_max_pixels();
+
 }  // namespace aq

@@ -19,6 +19,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 #include "internal.h"
 
@@ -652,6 +654,169 @@ void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, 
             stats->shade_ms = ts.total_ms();
             stats->shadow_ms = tsh.total_ms();
         }
+    }
+}
+
+// ---------------------------------------------------------------- no-allocation variant
+// Some callers cannot let a library call cudaMalloc: engines that own all
+// device memory through their own arena and a fixed budget, and hosts where
+// the implicit device synchronisation of cudaMalloc/cudaFree would stall
+// other work on the GPU. For them this variant runs the same wavefront
+// kernels on a fixed scratch area that lives in this file as a static device
+// array, so a render call allocates nothing. The caller still passes the
+// scene (loaded earlier) and a device buffer for the image.
+//
+// Scratch layout: path state for kNoAllocSlots slots (ray origin, direction,
+// hit, throughput, rng/work/depth: 16 B each; two 4 B queues; a 48 B shadow
+// record) + a 16 B film entry for up to kNoAllocPixels pixels + counters.
+// Every GPU that loads this library holds the array (about 17.3 MB) until
+// the process exits. All calls share it and it keeps the last call's
+// contents; each call clears the film, counters and statistics it needs.
+// Calls whose work overlaps on the GPU (two contexts or streams at once)
+// race on the array.
+constexpr size_t kNoAllocSlots = (size_t)1 << 16;
+constexpr size_t kNoAllocPixels = (size_t)1 << 19;
+constexpr size_t kNoAllocCounters = 64;  // uint32, >= kCntBucket0 + 8
+constexpr size_t kNoAllocStats = 16;     // uint64
+constexpr size_t kNoAllocStateBytes = kNoAllocSlots * (5 * 16 + 2 * 4 + 3 * 16);
+constexpr size_t kNoAllocBytes =
+    kNoAllocStateBytes + kNoAllocPixels * 16 + kNoAllocCounters * 4 + kNoAllocStats * 8;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_base[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device. In host code
+// `g_noalloc_scratch` names a host-side stand-in, not device memory, so the
+// address is looked up once per device (the first call on that device does
+// it, which also loads the module that holds the array) and cached.
+void* noalloc_base(int device) {
+    if (device < 0 || device >= kNoAllocMaxDevices)
+        throw Error(AQUA_ERR_UNSUPPORTED, "device ordinal beyond the no-allocation table");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_base[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            throw Error(AQUA_ERR_CUDA, std::string("cudaGetSymbolAddress(no-allocation scratch): ") +
+                                           cudaGetErrorString(e));
+        g_noalloc_base[device] = p;
+    }
+    return g_noalloc_base[device];
+}
+}  // namespace
+
+size_t render_noalloc_max_pixels() { return kNoAllocPixels; }
+
+void render_noalloc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, float* rgb_out,
+                    aqua_stats* stats) {
+    const DevScene& S = sc->ds;
+    if (cfg.spp <= 0) throw Error(AQUA_ERR_INVALID_ARG, "spp must be positive");
+    if (cfg.max_depth < 0) throw Error(AQUA_ERR_INVALID_ARG, "max_depth must be >= 0");
+    size_t pixels = (size_t)S.cam.width * (size_t)S.cam.height;
+    if (pixels == 0) throw Error(AQUA_ERR_INVALID_ARG, "resolution out of range");
+    if (pixels > kNoAllocPixels)
+        throw Error(AQUA_ERR_INVALID_ARG, "aqua_render_noalloc: " + std::to_string(pixels) +
+                                              " pixels exceed the fixed scratch limit of " +
+                                              std::to_string(kNoAllocPixels) + " pixels");
+    size_t slots = std::min(pixels, kNoAllocSlots);
+    if ((uint64_t)cfg.spp * ((pixels + slots - 1) / slots) > 0xFFFFFFFFull)
+        throw Error(AQUA_ERR_INVALID_ARG, "spp x pixels per slot exceeds 2^32");
+    if (((uintptr_t)rgb_out & 3) != 0) throw Error(AQUA_ERR_INVALID_ARG, "rgb_out must be 4-byte aligned");
+    char* base = (char*)noalloc_base(ctx->device);
+    cudaStream_t st = ctx->stream;
+
+    WaveParams P;
+    P.seed = cfg.seed;
+    P.spp = cfg.spp;
+    P.spp_offset = cfg.spp_offset;
+    P.max_depth = cfg.max_depth;
+    P.rr_depth = cfg.rr_depth;
+    P.slots = (uint32_t)slots;
+    P.pixels = (uint32_t)pixels;
+    P.nb = 0;  // unsorted shading: no per-material buckets
+    WavePtrs W;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char* p = base + off; off += bytes; return p; };
+    W.ray_o = (float4*)take(16 * kNoAllocSlots);
+    W.ray_d = (float4*)take(16 * kNoAllocSlots);
+    W.hit = (float4*)take(16 * kNoAllocSlots);
+    W.tp = (float4*)take(16 * kNoAllocSlots);
+    W.pst = (uint4*)take(16 * kNoAllocSlots);
+    uint32_t* q[2];
+    q[0] = (uint32_t*)take(4 * kNoAllocSlots);
+    q[1] = (uint32_t*)take(4 * kNoAllocSlots);
+    W.sh_o = (float4*)take(16 * kNoAllocSlots);
+    W.sh_d = (float4*)take(16 * kNoAllocSlots);
+    W.sh_c = (float4*)take(16 * kNoAllocSlots);
+    W.film = (float4*)take(16 * kNoAllocPixels);
+    W.counters = (uint32_t*)take(4 * kNoAllocCounters);
+    W.stats = (unsigned long long*)take(8 * kNoAllocStats);
+    W.bucket = nullptr;
+
+    // Leftovers of the previous call must not leak into this one.
+    AQ_CUDA(cudaMemsetAsync(W.film, 0, 16 * pixels, st));
+    AQ_CUDA(cudaMemsetAsync(W.counters, 0, 4 * kNoAllocCounters, st));
+    AQ_CUDA(cudaMemsetAsync(W.stats, 0, 8 * kNoAllocStats, st));
+
+    auto trace_k = k_trace_ext<false, false>;
+    auto shade_k = k_shade<false>;
+    auto shadow_k = k_shadow<false>;
+    int g_trace = grid_for(ctx, trace_k, 128, 0);
+    int g_shade = grid_for(ctx, shade_k, 128, 0);
+    int g_shadow = grid_for(ctx, shadow_k, 128, 0);
+    uint64_t launches = 0;
+    W.q_in = q[0];
+    W.q_out = q[1];
+    {
+        int g = (int)std::min<size_t>((slots + 255) / 256, (size_t)ctx->num_sms * 16);
+        k_raygen<<<std::max(g, 1), 256, 0, st>>>(S, P, W);
+        AQ_CUDA(cudaGetLastError());
+        ++launches;
+    }
+    const int chunk = 16;
+    const uint64_t max_iters =
+        (uint64_t)(cfg.max_depth + 2) * (uint64_t)cfg.spp * ((pixels + slots - 1) / slots) + 64;
+    uint64_t iter = 0;
+    unsigned int* pc = ctx->pinned_counter;  // pinned when the context was created
+    while (true) {
+        for (int k = 0; k < chunk; ++k, ++iter) {
+            uint32_t in = (uint32_t)(iter & 1), out = 1u - in;
+            W.q_in = q[in];
+            W.q_out = q[out];
+            trace_k<<<g_trace, 128, 0, st>>>(S, P, W, in, out);
+            shade_k<<<g_shade, 128, 0, st>>>(S, P, W, in, out);
+            shadow_k<<<g_shadow, 128, 0, st>>>(S, P, W);
+            launches += 3;
+        }
+        AQ_CUDA(cudaGetLastError());
+        AQ_CUDA(cudaMemcpyAsync(&pc[4], &W.counters[iter & 1], 4, cudaMemcpyDeviceToHost, st));
+        AQ_CUDA(cudaStreamSynchronize(st));
+        if (pc[4] == 0) break;
+        if (iter > max_iters) throw Error(AQUA_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");
+    }
+    {
+        int g = (int)std::min<size_t>((pixels + 255) / 256, (size_t)ctx->num_sms * 16);
+        k_resolve<<<g, 256, 0, st>>>(W.film, rgb_out, (uint32_t)pixels, 1.0f / (float)cfg.spp, 0);
+        AQ_CUDA(cudaGetLastError());
+        ++launches;
+    }
+    unsigned long long hs[kNoAllocStats];
+    AQ_CUDA(cudaMemcpyAsync(hs, W.stats, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    AQ_CUDA(cudaStreamSynchronize(st));
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->paths = hs[kStatPaths];
+        stats->ext_rays = hs[kStatExt];
+        stats->shadow_rays = hs[kStatShadow];
+        stats->iterations = iter;
+        stats->trace_launches = iter;
+        stats->shade_launches = iter;
+        stats->shadow_launches = iter;
+        stats->total_launches = launches;
     }
 }
 

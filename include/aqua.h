@@ -303,6 +303,30 @@ AQUA_API aqua_status aqua_render_batch(aqua_ctx* ctx, const aqua_job* jobs, size
 /* Device memory currently held by the context's render workspace. */
 AQUA_API uint64_t aqua_workspace_bytes(const aqua_ctx* ctx);
 
+/* aqua_render without any device allocation. No counterpart in the
+ * reference: it exists for callers that may not let a library call
+ * cudaMalloc — engines that hand out all device memory from their own arena
+ * under a fixed budget, and hosts where the implicit device-wide
+ * synchronisation of cudaMalloc/cudaFree would stall other GPU work.
+ *
+ * It renders like aqua_render (path integrator, same image bit for bit) but
+ * keeps all scratch — path state, queues, film — in one static device array
+ * of this library (about 17.3 MB, held by every GPU that loads the library
+ * until the process exits). The scene must already be loaded and
+ * rgb_out_device is a device buffer of width*height*3 floats owned by the
+ * caller. Limits: at most aqua_render_noalloc_max_pixels() pixels (2^19),
+ * else AQUA_ERR_INVALID_ARG before any device work.
+ *
+ * The first call on a device looks up the array's device address (a
+ * one-time set-up per device); make that first call before any stream
+ * capture. Every call shares the array and clears what it needs; calls
+ * whose work overlaps on the GPU (other contexts or threads at the same
+ * time) race on it and must be serialised by the caller. stats may be NULL;
+ * its timing fields stay 0. */
+AQUA_API aqua_status aqua_render_noalloc(aqua_ctx* ctx, aqua_scene* scene, const aqua_integrator_cfg* cfg,
+                                         float* rgb_out_device, aqua_stats* stats);
+AQUA_API uint64_t aqua_render_noalloc_max_pixels(void);
+
 #ifdef __cplusplus
 }
 #endif
