@@ -153,7 +153,82 @@ SIGNATURES = [
     ("aqua_workspace_bytes", C.c_uint64, [_P]),
     ("aqua_render_noalloc", C.c_int, [_P, _P, C.POINTER(IntegratorCfg), _P, C.POINTER(Stats)]),
     ("aqua_render_noalloc_max_pixels", C.c_uint64, []),
+    ("aqua_nrc_defaults", None, [_P]),
+    ("aqua_nrc_create", C.c_int, [_P, _P, C.POINTER(_P)]),
+    ("aqua_nrc_destroy", C.c_int, [_P, _P]),
+    ("aqua_nrc_set_weights", C.c_int, [_P, _P, _P]),
+    ("aqua_nrc_get_weights", C.c_int, [_P, _P, _P]),
+    ("aqua_nrc_get_gradients", C.c_int, [_P, _P, _P]),
+    ("aqua_nrc_encode", C.c_int, [_P, _P, _P, C.c_size_t, _P, C.c_uint32]),
+    ("aqua_nrc_forward", C.c_int, [_P, _P, _P, C.c_size_t, _P, C.c_uint32]),
+    ("aqua_nrc_train_step", C.c_int, [_P, _P, _P, _P, C.c_size_t, C.POINTER(C.c_double), C.c_uint32]),
 ]
+
+NRC_PARAMS = 20672
+
+
+class NrcCfg(C.Structure):
+    _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
+                ("seed", C.c_uint64), ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3)]
+
+
+class Nrc:
+    """The radiance cache's network (weights + Adam state) on the context's device."""
+
+    def __init__(self, ctx: "Context", **over):
+        self.ctx = ctx
+        cfg = NrcCfg()
+        ctx.lib.aqua_nrc_defaults(C.byref(cfg))
+        for k, v in over.items():
+            if k in ("bbox_min", "bbox_max"):
+                getattr(cfg, k)[:] = list(v)
+            else:
+                setattr(cfg, k, v)
+        h = C.c_void_p()
+        ctx._check(ctx.lib.aqua_nrc_create(ctx.handle, C.byref(cfg), C.byref(h)))
+        self.handle = h.value
+
+    def free(self):
+        if self.handle:
+            self.ctx._check(self.ctx.lib.aqua_nrc_destroy(self.ctx.handle, self.handle))
+            self.handle = None
+
+    def weights(self) -> np.ndarray:
+        w = np.zeros(NRC_PARAMS, np.float32)
+        self.ctx._check(self.ctx.lib.aqua_nrc_get_weights(self.ctx.handle, self.handle, _ptr(w)))
+        return w
+
+    def set_weights(self, w: np.ndarray):
+        w = np.ascontiguousarray(w, np.float32)
+        assert w.size == NRC_PARAMS
+        self.ctx._check(self.ctx.lib.aqua_nrc_set_weights(self.ctx.handle, self.handle, _ptr(w)))
+
+    def gradients(self) -> np.ndarray:
+        g = np.zeros(NRC_PARAMS, np.float32)
+        self.ctx._check(self.ctx.lib.aqua_nrc_get_gradients(self.ctx.handle, self.handle, _ptr(g)))
+        return g
+
+    def encode(self, raw: np.ndarray) -> np.ndarray:
+        raw = np.ascontiguousarray(raw, np.float32).reshape(-1, 16)
+        x = np.zeros((raw.shape[0], 64), np.uint16)
+        self.ctx._check(self.ctx.lib.aqua_nrc_encode(self.ctx.handle, self.handle, _ptr(raw), raw.shape[0],
+                                                     _ptr(x), 0))
+        return x
+
+    def forward(self, x_bf16: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x_bf16, np.uint16).reshape(-1, 64)
+        out = np.zeros((x.shape[0], 3), np.float32)
+        self.ctx._check(self.ctx.lib.aqua_nrc_forward(self.ctx.handle, self.handle, _ptr(x), x.shape[0],
+                                                      _ptr(out), 0))
+        return out
+
+    def train_step(self, x_bf16: np.ndarray, target: np.ndarray) -> float:
+        x = np.ascontiguousarray(x_bf16, np.uint16).reshape(-1, 64)
+        t = np.ascontiguousarray(target, np.float32).reshape(-1, 3)
+        loss = C.c_double()
+        self.ctx._check(self.ctx.lib.aqua_nrc_train_step(self.ctx.handle, self.handle, _ptr(x), _ptr(t),
+                                                         x.shape[0], C.byref(loss), 0))
+        return loss.value
 
 _lib = None
 

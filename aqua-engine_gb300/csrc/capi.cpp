@@ -8,6 +8,7 @@
 #include <new>
 
 #include "internal.h"
+#include "nrc.h"
 
 namespace {
 thread_local std::string g_create_error;
@@ -517,5 +518,167 @@ AQUA_API aqua_status aqua_render_noalloc(aqua_ctx* ctx, aqua_scene* s, const aqu
 }
 
 AQUA_API uint64_t aqua_render_noalloc_max_pixels(void) { return (uint64_t)render_noalloc_max_pixels(); }
+
+// ---------------------------------------------------------------- radiance cache
+static_assert(AQUA_NRC_PARAMS == kNrcParams, "parameter count");
+static_assert(AQUA_NRC_RAW == kNrcRaw, "raw feature count");
+
+static void stage(aqua_ctx* ctx, DevBuf& b, size_t bytes) {
+    if (b.bytes >= bytes && b.ptr) return;
+    dev_free(b);
+    dev_alloc(ctx, b, bytes);
+}
+
+AQUA_API void aqua_nrc_defaults(aqua_nrc_cfg* c) {
+    if (!c) return;
+    memset(c, 0, sizeof(*c));
+    c->learning_rate = 1e-2f;
+    c->beta1 = 0.9f;
+    c->beta2 = 0.99f;
+    c->eps = 1e-8f;
+    c->seed = 1;
+    for (int i = 0; i < 3; ++i) { c->bbox_min[i] = 0.0f; c->bbox_max[i] = 1.0f; }
+}
+
+AQUA_API aqua_status aqua_nrc_create(aqua_ctx* ctx, const aqua_nrc_cfg* cfg, aqua_nrc** out) {
+    return guard(ctx, [&]() {
+        need(out != nullptr, "out must be non-NULL");
+        need_device(ctx);
+        *out = nullptr;
+        aqua_nrc_cfg c;
+        if (cfg) c = *cfg;
+        else aqua_nrc_defaults(&c);
+        for (int i = 0; i < 3; ++i)
+            need(c.bbox_max[i] > c.bbox_min[i], "bbox_max must exceed bbox_min on every axis");
+        need(c.learning_rate > 0.0f, "learning_rate must be positive");
+        aqua_nrc* n = new aqua_nrc();
+        try {
+            n->net.lr = c.learning_rate;
+            n->net.beta1 = c.beta1;
+            n->net.beta2 = c.beta2;
+            n->net.eps = c.eps;
+            for (int i = 0; i < 3; ++i) {
+                n->net.bmin[i] = c.bbox_min[i];
+                n->net.bext[i] = c.bbox_max[i] - c.bbox_min[i];
+            }
+            nrc_alloc(ctx, n->net);
+            nrc_init_weights(ctx, n->net, c.seed);
+        } catch (...) {
+            nrc_release(n->net);
+            delete n;
+            throw;
+        }
+        *out = n;
+    });
+}
+
+AQUA_API aqua_status aqua_nrc_destroy(aqua_ctx* ctx, aqua_nrc* n) {
+    return guard(ctx, [&]() {
+        if (!n) return;
+        cudaStreamSynchronize(ctx->stream);
+        nrc_release(n->net);
+        dev_free(n->stage_in);
+        dev_free(n->stage_tgt);
+        dev_free(n->stage_out);
+        delete n;
+    });
+}
+
+AQUA_API aqua_status aqua_nrc_set_weights(aqua_ctx* ctx, aqua_nrc* n, const float* w) {
+    return guard(ctx, [&]() {
+        need(n && w, "nrc and w must be non-NULL");
+        nrc_set_weights(ctx, n->net, w);
+    });
+}
+
+AQUA_API aqua_status aqua_nrc_get_weights(aqua_ctx* ctx, aqua_nrc* n, float* w) {
+    return guard(ctx, [&]() {
+        need(n && w, "nrc and w must be non-NULL");
+        AQ_CUDA(cudaMemcpyAsync(w, n->net.w, 4 * kNrcParams, cudaMemcpyDeviceToHost, ctx->stream));
+        AQ_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+AQUA_API aqua_status aqua_nrc_get_gradients(aqua_ctx* ctx, aqua_nrc* n, float* g) {
+    return guard(ctx, [&]() {
+        need(n && g, "nrc and g must be non-NULL");
+        AQ_CUDA(cudaMemcpyAsync(g, n->net.grad, 4 * kNrcParams, cudaMemcpyDeviceToHost, ctx->stream));
+        AQ_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+AQUA_API aqua_status aqua_nrc_encode(aqua_ctx* ctx, aqua_nrc* n, const float* raw, size_t cnt, uint16_t* x,
+                                     uint32_t flags) {
+    return guard(ctx, [&]() {
+        need(n != nullptr, "nrc is NULL");
+        need(cnt == 0 || (raw && x), "raw and x must be non-NULL");
+        need(cnt < (1u << 30), "too many rows");
+        if (cnt == 0) return;
+        const float* d_raw = raw;
+        uint16_t* d_x = x;
+        if (!(flags & AQUA_NRC_DEVICE_PTRS)) {
+            stage(ctx, n->stage_in, 4 * kNrcRaw * cnt);
+            stage(ctx, n->stage_out, 128 * cnt);
+            AQ_CUDA(cudaMemcpyAsync(n->stage_in.ptr, raw, 4 * kNrcRaw * cnt, cudaMemcpyHostToDevice, ctx->stream));
+            d_raw = (const float*)n->stage_in.ptr;
+            d_x = (uint16_t*)n->stage_out.ptr;
+        }
+        nrc_encode_dev(ctx, n->net, d_raw, (int)cnt, d_x);
+        if (!(flags & AQUA_NRC_DEVICE_PTRS))
+            AQ_CUDA(cudaMemcpyAsync(x, d_x, 128 * cnt, cudaMemcpyDeviceToHost, ctx->stream));
+        AQ_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+AQUA_API aqua_status aqua_nrc_forward(aqua_ctx* ctx, aqua_nrc* n, const uint16_t* x, size_t cnt, float* out,
+                                      uint32_t flags) {
+    return guard(ctx, [&]() {
+        need(n != nullptr, "nrc is NULL");
+        need(cnt == 0 || (x && out), "x and out must be non-NULL");
+        need(cnt < (1u << 30), "too many rows");
+        if (cnt == 0) return;
+        const uint16_t* d_x = x;
+        float* d_out = out;
+        if (!(flags & AQUA_NRC_DEVICE_PTRS)) {
+            stage(ctx, n->stage_in, 128 * cnt);
+            stage(ctx, n->stage_out, 12 * cnt);
+            AQ_CUDA(cudaMemcpyAsync(n->stage_in.ptr, x, 128 * cnt, cudaMemcpyHostToDevice, ctx->stream));
+            d_x = (const uint16_t*)n->stage_in.ptr;
+            d_out = (float*)n->stage_out.ptr;
+        } else {
+            need(((uintptr_t)x & 15) == 0, "x must be 16-byte aligned");
+        }
+        nrc_forward_dev(ctx, n->net, d_x, (int)cnt, d_out);
+        if (!(flags & AQUA_NRC_DEVICE_PTRS))
+            AQ_CUDA(cudaMemcpyAsync(out, d_out, 12 * cnt, cudaMemcpyDeviceToHost, ctx->stream));
+        AQ_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+AQUA_API aqua_status aqua_nrc_train_step(aqua_ctx* ctx, aqua_nrc* n, const uint16_t* x, const float* target,
+                                         size_t cnt, double* loss, uint32_t flags) {
+    return guard(ctx, [&]() {
+        need(n != nullptr, "nrc is NULL");
+        need(cnt > 0 && x && target, "x and target must be non-NULL and n > 0");
+        need(cnt < (1u << 26), "too many rows");
+        const uint16_t* d_x = x;
+        const float* d_t = target;
+        if (!(flags & AQUA_NRC_DEVICE_PTRS)) {
+            stage(ctx, n->stage_in, 128 * cnt);
+            stage(ctx, n->stage_tgt, 12 * cnt);
+            AQ_CUDA(cudaMemcpyAsync(n->stage_in.ptr, x, 128 * cnt, cudaMemcpyHostToDevice, ctx->stream));
+            AQ_CUDA(cudaMemcpyAsync(n->stage_tgt.ptr, target, 12 * cnt, cudaMemcpyHostToDevice, ctx->stream));
+            d_x = (const uint16_t*)n->stage_in.ptr;
+            d_t = (const float*)n->stage_tgt.ptr;
+        } else {
+            need(((uintptr_t)x & 15) == 0, "x must be 16-byte aligned");
+        }
+        nrc_train_step_dev(ctx, n->net, d_x, d_t, (int)cnt);
+        double l = 0.0;
+        AQ_CUDA(cudaMemcpyAsync(&l, n->net.loss, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        AQ_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (loss) *loss = l / (double)(cnt * kNrcOut);
+    });
+}
 
 }  // extern "C"

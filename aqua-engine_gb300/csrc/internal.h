@@ -58,6 +58,30 @@ struct Workspace {
     float* out_rgb = nullptr;  // staging for host films (pixels * 3)
 };
 
+// Radiance-cache network: FP32 master weights + Adam state, bf16 fragment
+// tables for the tensor-core kernels, and training scratch.
+struct NrcNet {
+    DevBuf block;            // weights, Adam moments, gradient, fragments, loss
+    float* w = nullptr;      // master weights [W1..W5 64x64, W6 3x64]
+    float* m = nullptr;
+    float* v = nullptr;
+    float* grad = nullptr;   // last step's gradient
+    uint2* frag = nullptr;   // forward B fragments
+    uint2* fragT = nullptr;  // backward B fragments
+    double* loss = nullptr;  // loss sum of the last step
+    DevBuf train;            // training scratch, sized by train_rows
+    int train_rows = 0;
+    float* ty = nullptr;       // forward outputs (rows x 3)
+    uint32_t* acts = nullptr;  // H1..H5 bf16 (5 x rows x 64)
+    uint32_t* deltas = nullptr;// delta1..delta5 bf16 (5 x rows x 64)
+    uint32_t* d6 = nullptr;    // dY bf16 (rows x 16)
+    float* partial = nullptr;  // per-chunk weight gradients
+    int64_t step = 0;
+    float lr = 1e-2f, beta1 = 0.9f, beta2 = 0.99f, eps = 1e-8f;
+    float bmin[3] = {0, 0, 0}, bext[3] = {1, 1, 1};
+    uint64_t launches = 0;
+};
+
 enum { kCntQ0 = 0, kCntQ1 = 1, kCntShadow = 2, kCntBucket0 = 8 };
 enum { kStatExt = 0, kStatShadow, kStatPaths, kStatNodes, kStatTris, kStatShNodes, kStatShTris, kStatCount };
 
@@ -72,6 +96,11 @@ struct aqua_scene {
     aq::DevBuf dev;            // device copy
     aq::DevScene ds{};         // pointers into dev
     bool uploaded = false;
+};
+
+struct aqua_nrc {
+    aq::NrcNet net;
+    aq::DevBuf stage_in, stage_tgt, stage_out;  // staging for host-pointer calls
 };
 
 struct aqua_ctx {
@@ -108,6 +137,16 @@ void trace_rays(aqua_ctx* ctx, aqua_scene* s, const aqua_ray* rays, size_t n, aq
 void render_path(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg& cfg, const aqua_tuning& tune,
                  float* rgb_out, uint32_t flags, aqua_stats* stats);
 void workspace_release(aqua_ctx* ctx);
+
+// Radiance-cache network (nrc.cu).
+void nrc_alloc(aqua_ctx* ctx, NrcNet& net);
+void nrc_release(NrcNet& net);
+void nrc_init_weights(aqua_ctx* ctx, NrcNet& net, uint64_t seed);
+void nrc_set_weights(aqua_ctx* ctx, NrcNet& net, const float* host_w);
+void nrc_pack(aqua_ctx* ctx, NrcNet& net);
+void nrc_forward_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, int n, float* out);
+void nrc_train_step_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, const float* target, int n);
+void nrc_encode_dev(aqua_ctx* ctx, NrcNet& net, const float* raw, int n, uint16_t* X);
 
 // Render on the library's fixed static scratch array; no device allocation.
 void render_noalloc(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg& cfg, float* rgb_out,

@@ -303,6 +303,44 @@ AQUA_API aqua_status aqua_render_batch(aqua_ctx* ctx, const aqua_job* jobs, size
 /* Device memory currently held by the context's render workspace. */
 AQUA_API uint64_t aqua_workspace_bytes(const aqua_ctx* ctx);
 
+/* ---------------------------------------------------------------- radiance cache */
+/* The network of the `"type": "nrc"` integrator (scenes/integrator.json:2-7):
+ * 64 encoded inputs -> 5 hidden layers of 64 (ReLU) -> RGB radiance, BF16
+ * weights and activations with FP32 accumulation on tensor cores, trained
+ * online with Adam on a relative L2 loss. Weights are FP32 row-major
+ * [out][in]: W1..W5 (64x64) then W6 (3x64), AQUA_NRC_PARAMS values. */
+typedef struct aqua_nrc aqua_nrc;
+
+enum { AQUA_NRC_PARAMS = 20672, AQUA_NRC_INPUTS = 64, AQUA_NRC_RAW = 16 };
+enum { AQUA_NRC_DEVICE_PTRS = 1u << 0 };
+
+typedef struct aqua_nrc_cfg {
+    float learning_rate;          /* Adam step size                         */
+    float beta1, beta2, eps;      /* Adam moments                           */
+    uint64_t seed;                /* He-uniform initial weights             */
+    float bbox_min[3], bbox_max[3]; /* box that normalises positions        */
+} aqua_nrc_cfg;
+
+AQUA_API void aqua_nrc_defaults(aqua_nrc_cfg* cfg);
+AQUA_API aqua_status aqua_nrc_create(aqua_ctx* ctx, const aqua_nrc_cfg* cfg, aqua_nrc** out);
+AQUA_API aqua_status aqua_nrc_destroy(aqua_ctx* ctx, aqua_nrc* nrc);
+/* Replaces the weights (and resets the Adam state). */
+AQUA_API aqua_status aqua_nrc_set_weights(aqua_ctx* ctx, aqua_nrc* nrc, const float* w);
+AQUA_API aqua_status aqua_nrc_get_weights(aqua_ctx* ctx, aqua_nrc* nrc, float* w);
+/* Gradient of the mean loss used by the last training step. */
+AQUA_API aqua_status aqua_nrc_get_gradients(aqua_ctx* ctx, aqua_nrc* nrc, float* g);
+/* raw: n x AQUA_NRC_RAW floats per vertex (position 3, outgoing direction 3,
+ * normal 3, roughness, diffuse albedo 3, specular F0 3); x: n x 64 bf16. */
+AQUA_API aqua_status aqua_nrc_encode(aqua_ctx* ctx, aqua_nrc* nrc, const float* raw, size_t n, uint16_t* x,
+                                     uint32_t flags);
+/* out: n x 3 floats (radiance). */
+AQUA_API aqua_status aqua_nrc_forward(aqua_ctx* ctx, aqua_nrc* nrc, const uint16_t* x, size_t n, float* out,
+                                      uint32_t flags);
+/* One Adam step on a batch of n records (x, target radiance n x 3); loss =
+ * the batch's mean relative L2 loss before the step (may be NULL). */
+AQUA_API aqua_status aqua_nrc_train_step(aqua_ctx* ctx, aqua_nrc* nrc, const uint16_t* x, const float* target,
+                                         size_t n, double* loss, uint32_t flags);
+
 /* aqua_render without any device allocation. No counterpart in the
  * reference: it exists for callers that may not let a library call
  * cudaMalloc — engines that hand out all device memory from their own arena

@@ -613,9 +613,170 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
     }
 }
 
+// ------------------------------------------------------------------ MLP
+// bfloat16 rounding, round to nearest even (finite inputs).
+double to_bf16(double v) {
+    float f = (float)v;
+    uint32_t b;
+    memcpy(&b, &f, 4);
+    b = (b + 0x7FFFu + ((b >> 16) & 1u)) & 0xFFFF0000u;
+    memcpy(&f, &b, 4);
+    return (double)f;
+}
+
+struct Mlp {
+    std::vector<double> W[6];  // W[l] row-major [out][in]
+    int outs(int l) const { return l == 5 ? 3 : 64; }
+    Mlp(const float* w, bool bf) {
+        for (int l = 0; l < 6; ++l) {
+            int o = outs(l);
+            W[l].resize((size_t)o * 64);
+            for (int i = 0; i < o * 64; ++i) {
+                double v = w[l * 4096 + i];
+                W[l][(size_t)i] = bf ? to_bf16(v) : v;
+            }
+        }
+    }
+    // h[0] = input, h[l+1] = relu(W_l h[l]) for l < 5; y = W_5 h[5].
+    void forward(const float* x, bool bf, double h[6][64], double y[3]) const {
+        for (int i = 0; i < 64; ++i) h[0][i] = bf ? to_bf16(x[i]) : (double)x[i];
+        for (int l = 0; l < 5; ++l)
+            for (int o = 0; o < 64; ++o) {
+                double z = 0.0;
+                for (int i = 0; i < 64; ++i) z += W[l][(size_t)o * 64 + i] * h[l][i];
+                z = z > 0.0 ? z : 0.0;
+                h[l + 1][o] = bf ? to_bf16(z) : z;
+            }
+        for (int o = 0; o < 3; ++o) {
+            double z = 0.0;
+            for (int i = 0; i < 64; ++i) z += W[5][(size_t)o * 64 + i] * h[5][i];
+            y[o] = z;
+        }
+    }
+};
+
+// Encoding of one vertex (restated from the definition in oracle.h).
+void encode_row(const float* r, const float* bmin, const float* bmax, float* x) {
+    double pn[3];
+    for (int a = 0; a < 3; ++a) {
+        double t = ((double)r[a] - bmin[a]) / ((double)bmax[a] - bmin[a]);
+        pn[a] = std::min(std::max(t, 0.0), 1.0);
+    }
+    auto sph = [](double x0, double y0, double z0, double& u, double& v) {
+        u = std::acos(std::min(std::max(z0, -1.0), 1.0)) / M_PI;
+        v = (std::atan2(y0, x0) + M_PI) / (2.0 * M_PI);
+        u = std::min(std::max(u, 0.0), 1.0);
+        v = std::min(std::max(v, 0.0), 1.0);
+    };
+    auto blob = [](double v, int b) {
+        double d = (v - (b + 0.5) / 4.0) * 4.0;
+        return std::exp(-0.5 * d * d);
+    };
+    double du, dv, nu, nv;
+    sph(r[3], r[4], r[5], du, dv);
+    sph(r[6], r[7], r[8], nu, nv);
+    double rough = std::min(std::max((double)r[9], 0.0), 1.0);
+    for (int c = 0; c < 64; ++c) {
+        double v;
+        if (c < 36) {
+            int axis = c / 12, f = (c % 12) / 2;
+            double a = pn[axis] * (double)(1 << f) * M_PI;
+            v = (c & 1) ? std::cos(a) : std::sin(a);
+        } else if (c < 44) {
+            int k = c - 36;
+            v = blob(k < 4 ? du : dv, k & 3);
+        } else if (c < 52) {
+            int k = c - 44;
+            v = blob(k < 4 ? nu : nv, k & 3);
+        } else if (c < 56) {
+            v = blob(rough, c - 52);
+        } else if (c < 59) {
+            v = r[10 + (c - 56)];
+        } else if (c < 62) {
+            v = r[13 + (c - 59)];
+        } else {
+            v = c == 62 ? 1.0 : 0.0;
+        }
+        x[c] = (float)v;
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+void orc_mlp_forward(const float* w, const float* x, int64_t n, int emulate_bf16, float* out) {
+    Mlp net(w, emulate_bf16 != 0);
+    parallel_for(n, 0, [&](int64_t r) {
+        double h[6][64], y[3];
+        net.forward(x + 64 * r, emulate_bf16 != 0, h, y);
+        for (int c = 0; c < 3; ++c) out[3 * r + c] = (float)y[c];
+    });
+}
+
+void orc_mlp_forward_f64(const float* w, const float* x, int64_t n, int emulate_bf16, double* out) {
+    Mlp net(w, emulate_bf16 != 0);
+    parallel_for(n, 0, [&](int64_t r) {
+        double h[6][64], y[3];
+        net.forward(x + 64 * r, emulate_bf16 != 0, h, y);
+        for (int c = 0; c < 3; ++c) out[3 * r + c] = y[c];
+    });
+}
+
+void orc_mlp_grad(const float* w, const float* x, const float* target, int64_t n, int emulate_bf16, double* grad,
+                  double* loss) {
+    const bool bf = emulate_bf16 != 0;
+    Mlp net(w, bf);
+    const double inv = 1.0 / (3.0 * (double)n);
+    // Per-thread accumulation over fixed row blocks, summed in block order.
+    const int64_t block = 256;
+    int64_t nb = (n + block - 1) / block;
+    std::vector<std::vector<double>> part((size_t)nb, std::vector<double>(AQUA_NRC_PARAMS + 1, 0.0));
+    parallel_for(nb, 0, [&](int64_t b) {
+        std::vector<double>& g = part[(size_t)b];
+        for (int64_t r = b * block; r < std::min(n, (b + 1) * block); ++r) {
+            double h[6][64], y[3], d[64], dn[64];
+            net.forward(x + 64 * r, bf, h, y);
+            double dy[3];
+            for (int c = 0; c < 3; ++c) {
+                double t = target[3 * r + c], den = y[c] * y[c] + 0.01, e = y[c] - t;
+                g[AQUA_NRC_PARAMS] += e * e / den;
+                dy[c] = 2.0 * e / den * inv;
+                if (bf) dy[c] = to_bf16(dy[c]);
+            }
+            for (int o = 0; o < 3; ++o)
+                for (int i = 0; i < 64; ++i) g[(size_t)(5 * 4096 + o * 64 + i)] += dy[o] * h[5][i];
+            for (int i = 0; i < 64; ++i) {
+                double s = 0.0;
+                for (int o = 0; o < 3; ++o) s += net.W[5][(size_t)o * 64 + i] * dy[o];
+                d[i] = h[5][i] > 0.0 ? s : 0.0;
+                if (bf) d[i] = to_bf16(d[i]);
+            }
+            for (int l = 4; l >= 0; --l) {  // d = dL/dZ_l (delta of layer l+1)
+                for (int o = 0; o < 64; ++o)
+                    for (int i = 0; i < 64; ++i) g[(size_t)(l * 4096 + o * 64 + i)] += d[o] * h[l][i];
+                if (l == 0) break;
+                for (int i = 0; i < 64; ++i) {
+                    double s = 0.0;
+                    for (int o = 0; o < 64; ++o) s += net.W[l][(size_t)o * 64 + i] * d[o];
+                    dn[i] = h[l][i] > 0.0 ? s : 0.0;
+                    if (bf) dn[i] = to_bf16(dn[i]);
+                }
+                memcpy(d, dn, sizeof(d));
+            }
+        }
+    });
+    for (int p = 0; p <= AQUA_NRC_PARAMS; ++p) {
+        double s = 0.0;
+        for (int64_t b = 0; b < nb; ++b) s += part[(size_t)b][(size_t)p];
+        if (p < AQUA_NRC_PARAMS) grad[p] = s;
+        else if (loss) *loss = s * inv;
+    }
+}
+
+void orc_nrc_encode(const float* raw, int64_t n, const float* bmin, const float* bmax, float* x) {
+    parallel_for(n, 0, [&](int64_t r) { encode_row(raw + 16 * r, bmin, bmax, x + 64 * r); });
+}
 
 double orc_srgb_to_linear(double c) { return c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4); }
 

@@ -70,6 +70,22 @@ int orc_render(const orc_scene* s, int precision, int32_t spp, int32_t spp_offse
                int32_t rr_depth, uint64_t seed, int threads, int64_t pixel_begin, int64_t pixel_end,
                float* out, double* stats);
 
+/* Radiance-cache network (64 -> 5 x 64 ReLU -> 3, no biases; weights FP32
+ * row-major [out][in], W1..W5 then W6: 20,672 values), in double.
+ * emulate_bf16 = 1 rounds weights, inputs, stored activations and stored
+ * gradients to bfloat16 (round to nearest even) where the device kernels
+ * store them, so the only remaining difference is accumulation order.
+ * x: n x 64 floats. out: n x 3. */
+void orc_mlp_forward(const float* w, const float* x, int64_t n, int emulate_bf16, float* out);
+void orc_mlp_forward_f64(const float* w, const float* x, int64_t n, int emulate_bf16, double* out);
+/* Gradient of the mean relative L2 loss, mean over n x 3 of
+ * (y - t)^2 / (y^2 + 0.01) with the denominator held constant (Mueller et al.
+ * 2021), w.r.t. every weight; loss = that mean. */
+void orc_mlp_grad(const float* w, const float* x, const float* target, int64_t n, int emulate_bf16,
+                  double* grad, double* loss);
+/* Input encoding of raw vertex features (16 floats each) to 64 floats. */
+void orc_nrc_encode(const float* raw, int64_t n, const float* bmin, const float* bmax, float* x);
+
 /* Reference values the tests print. */
 double orc_srgb_to_linear(double c);
 uint32_t orc_pcg32_first(uint64_t initstate, uint64_t initseq, uint32_t* out, int n);

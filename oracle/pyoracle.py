@@ -51,6 +51,10 @@ def lib():
         L.orc_srgb_to_linear.restype = C.c_double
         L.orc_pcg32_first.argtypes = [C.c_uint64, C.c_uint64, P, C.c_int]
         L.orc_pcg32_first.restype = C.c_uint32
+        L.orc_mlp_forward.argtypes = [P, P, C.c_int64, C.c_int, P]
+        L.orc_mlp_forward_f64.argtypes = [P, P, C.c_int64, C.c_int, P]
+        L.orc_mlp_grad.argtypes = [P, P, P, C.c_int64, C.c_int, P, P]
+        L.orc_nrc_encode.argtypes = [P, C.c_int64, P, P, P]
         _lib = L
     return _lib
 
@@ -142,6 +146,59 @@ def pcg32_sequence(initstate: int, initseq: int, n: int) -> np.ndarray:
     out = np.zeros(n, np.uint32)
     lib().orc_pcg32_first(initstate, initseq, _p(out), n)
     return out
+
+
+NRC_PARAMS = 20672
+
+
+def mlp_forward(w: np.ndarray, x: np.ndarray, emulate_bf16: bool = True) -> np.ndarray:
+    w = np.ascontiguousarray(w, np.float32)
+    x = np.ascontiguousarray(x, np.float32).reshape(-1, 64)
+    out = np.zeros((x.shape[0], 3), np.float32)
+    lib().orc_mlp_forward(_p(w), _p(x), x.shape[0], int(emulate_bf16), _p(out))
+    return out
+
+
+def mlp_forward_f64(w: np.ndarray, x: np.ndarray, emulate_bf16: bool = False) -> np.ndarray:
+    w = np.ascontiguousarray(w, np.float32)
+    x = np.ascontiguousarray(x, np.float32).reshape(-1, 64)
+    out = np.zeros((x.shape[0], 3), np.float64)
+    lib().orc_mlp_forward_f64(_p(w), _p(x), x.shape[0], int(emulate_bf16), _p(out))
+    return out
+
+
+def mlp_grad(w: np.ndarray, x: np.ndarray, target: np.ndarray, emulate_bf16: bool = True):
+    w = np.ascontiguousarray(w, np.float32)
+    x = np.ascontiguousarray(x, np.float32).reshape(-1, 64)
+    t = np.ascontiguousarray(target, np.float32).reshape(-1, 3)
+    g = np.zeros(NRC_PARAMS, np.float64)
+    loss = C.c_double()
+    lib().orc_mlp_grad(_p(w), _p(x), _p(t), x.shape[0], int(emulate_bf16), _p(g), C.byref(loss))
+    return g, loss.value
+
+
+def nrc_encode(raw: np.ndarray, bmin, bmax) -> np.ndarray:
+    raw = np.ascontiguousarray(raw, np.float32).reshape(-1, 16)
+    bmin = np.ascontiguousarray(bmin, np.float32)
+    bmax = np.ascontiguousarray(bmax, np.float32)
+    x = np.zeros((raw.shape[0], 64), np.float32)
+    lib().orc_nrc_encode(_p(raw), raw.shape[0], _p(bmin), _p(bmax), _p(x))
+    return x
+
+
+def bf16_round(a: np.ndarray) -> np.ndarray:
+    """Round float32 values to bfloat16 (nearest even), returned as float32."""
+    b = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    b = (b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000
+    return b.astype(np.uint32).view(np.float32)
+
+
+def bf16_bits(a: np.ndarray) -> np.ndarray:
+    return (bf16_round(a).view(np.uint32) >> 16).astype(np.uint16)
+
+
+def bf16_to_float(bits: np.ndarray) -> np.ndarray:
+    return (np.asarray(bits, np.uint16).astype(np.uint32) << 16).view(np.float32)
 
 
 def rel_mse(x: np.ndarray, ref: np.ndarray) -> float:

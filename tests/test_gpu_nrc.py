@@ -1,0 +1,136 @@
+"""The radiance cache's network on the GPU against the FP64 CPU oracle.
+
+The oracle emulates the device's bf16 storage points (weights, inputs,
+activations, gradients), so the remaining differences are FP32 vs FP64
+accumulation and the rare bf16 rounding flips they cause. Tolerances:
+forward outputs within 1e-2 of the output scale; gradients within 2e-2
+relative L2 and cosine > 0.999; Adam bit-close to its closed form.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rand_raw(n, seed):
+    rng = np.random.default_rng(seed)
+    raw = np.zeros((n, 16), np.float32)
+    raw[:, 0:3] = rng.uniform(-1, 1, (n, 3))
+    for sl in (slice(3, 6), slice(6, 9)):
+        v = rng.normal(size=(n, 3))
+        raw[:, sl] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    raw[:, 9] = rng.uniform(0, 1, n)
+    raw[:, 10:16] = rng.uniform(0, 1, (n, 6))
+    return raw
+
+
+def smooth_target(raw):
+    p = raw[:, 0:3]
+    return np.stack([1.0 + 0.5 * np.sin(3 * p[:, 0]) * raw[:, 10],
+                     0.5 + 0.3 * np.cos(2 * p[:, 1] + p[:, 2]),
+                     np.abs(p[:, 2]) * raw[:, 12] + 0.2], axis=1).astype(np.float32)
+
+
+@pytest.fixture()
+def net(gpu_ctx):
+    import aqua
+
+    n = aqua.Nrc(gpu_ctx, seed=3, learning_rate=1e-2, bbox_min=[-1, -1, -1], bbox_max=[1, 1, 1])
+    yield n
+    n.free()
+
+
+def test_encode_matches_oracle(net):
+    import pyoracle
+
+    raw = rand_raw(5000, 1)
+    x = net.encode(raw)
+    ref = pyoracle.nrc_encode(raw, [-1, -1, -1], [1, 1, 1])
+    got = pyoracle.bf16_to_float(x)
+    # bf16 keeps 8 significant bits; the device's sin/cos/exp add ~1e-6.
+    assert np.all(np.abs(got - ref) <= 2 ** -8 * np.abs(ref) + 1e-5)
+
+
+def test_forward_matches_oracle(net):
+    import pyoracle
+
+    raw = rand_raw(4099, 2)  # not a multiple of 16: exercises the ragged tile
+    x = net.encode(raw)
+    w = net.weights()
+    y = net.forward(x)
+    ref = pyoracle.mlp_forward(w, pyoracle.bf16_to_float(x), emulate_bf16=True)
+    scale = np.abs(ref).max()
+    assert np.abs(y - ref).max() <= 1e-2 * scale
+    assert np.abs(y - ref).mean() <= 1e-3 * scale
+
+
+def test_gradient_matches_oracle(net):
+    import pyoracle
+
+    raw = rand_raw(8192 + 37, 3)
+    x = net.encode(raw)
+    t = smooth_target(raw)
+    w0 = net.weights()
+    loss = net.train_step(x, t)
+    g = net.gradients().astype(np.float64)
+    gref, lref = pyoracle.mlp_grad(w0, pyoracle.bf16_to_float(x), t, emulate_bf16=True)
+    assert abs(loss - lref) <= 1e-3 * lref
+    rel = np.linalg.norm(g - gref) / np.linalg.norm(gref)
+    cos = float(g @ gref / (np.linalg.norm(g) * np.linalg.norm(gref)))
+    assert rel < 2e-2 and cos > 0.999, (rel, cos)
+    # per layer too: every layer's gradient must agree, not just the total
+    for l in range(6):
+        sl = slice(l * 4096, l * 4096 + (4096 if l < 5 else 192))
+        r = np.linalg.norm(g[sl] - gref[sl]) / (np.linalg.norm(gref[sl]) + 1e-30)
+        assert r < 5e-2, (l, r)
+    # against the unquantised FP64 network: bf16 tolerance
+    g64, _ = pyoracle.mlp_grad(w0, pyoracle.bf16_to_float(x), t, emulate_bf16=False)
+    cos64 = float(g @ g64 / (np.linalg.norm(g) * np.linalg.norm(g64)))
+    assert cos64 > 0.99
+
+
+def test_adam_step_closed_form(net):
+    raw = rand_raw(2048, 4)
+    x = net.encode(raw)
+    t = smooth_target(raw)
+    w0 = net.weights().astype(np.float64)
+    net.train_step(x, t)
+    g = net.gradients().astype(np.float64)
+    w1 = net.weights().astype(np.float64)
+    lr, b1, b2, eps = 1e-2, 0.9, 0.99, 1e-8
+    m = (1 - b1) * g
+    v = (1 - b2) * g * g
+    expect = w0 - lr * (m / (1 - b1)) / (np.sqrt(v / (1 - b2)) + eps)
+    np.testing.assert_allclose(w1, expect, rtol=1e-4, atol=1e-6)
+
+
+def test_training_reduces_loss(net):
+    import pyoracle
+
+    raw = rand_raw(16384, 5)
+    x = net.encode(raw)
+    t = smooth_target(raw)
+    losses = [net.train_step(x[i % 4 * 4096:(i % 4 + 1) * 4096], t[i % 4 * 4096:(i % 4 + 1) * 4096])
+              for i in range(200)]
+    assert losses[-1] < 0.1 * losses[0]
+    held = rand_raw(2000, 6)
+    y = net.forward(net.encode(held))
+    th = smooth_target(held)
+    assert float(np.mean((y - th) ** 2 / (th ** 2 + 0.01))) < 0.02
+
+
+def test_set_weights_roundtrip_and_reset(net):
+    rng = np.random.default_rng(7)
+    w = (rng.uniform(-0.1, 0.1, 20672)).astype(np.float32)
+    net.set_weights(w)
+    np.testing.assert_array_equal(net.weights(), w)
+
+
+def test_bad_nrc_arguments(gpu_ctx):
+    import aqua
+
+    with pytest.raises(aqua.AquaError) as e:
+        aqua.Nrc(gpu_ctx, bbox_min=[0, 0, 0], bbox_max=[1, 0, 1])
+    assert e.value.status == aqua.ERR_INVALID_ARG
