@@ -162,6 +162,8 @@ SIGNATURES = [
     ("aqua_nrc_encode", C.c_int, [_P, _P, _P, C.c_size_t, _P, C.c_uint32]),
     ("aqua_nrc_forward", C.c_int, [_P, _P, _P, C.c_size_t, _P, C.c_uint32]),
     ("aqua_nrc_train_step", C.c_int, [_P, _P, _P, _P, C.c_size_t, C.POINTER(C.c_double), C.c_uint32]),
+    ("aqua_render_nrc", C.c_int, [_P, _P, C.POINTER(IntegratorCfg), C.POINTER(Tuning), _P, _P, C.c_uint32,
+                                  C.POINTER(Stats)]),
 ]
 
 NRC_PARAMS = 20672
@@ -396,6 +398,23 @@ class Context:
         self._check(self.lib.aqua_render(self.handle, scene.handle, C.byref(cfg),
                                          C.byref(tuning) if tuning is not None else None, _ptr(out), flags,
                                          C.byref(st)))
+        return out, st
+
+    def render_nrc(self, scene: Scene, cfg: IntegratorCfg, nrc: "Nrc", tuning: Tuning | None = None, flags: int = 0,
+                   out: np.ndarray | None = None, dev_ptr: int | None = None):
+        """One frame of the cached renderer (host film, or a device film with dev_ptr)."""
+        st = Stats()
+        if dev_ptr is not None:
+            target = C.c_void_p(dev_ptr)
+            flags |= RENDER_DEVICE_FILM
+        else:
+            inf = scene.info()
+            if out is None:
+                out = np.zeros((inf.height, inf.width, 3), np.float32)
+            target = _ptr(out)
+        self._check(self.lib.aqua_render_nrc(self.handle, scene.handle, C.byref(cfg),
+                                             C.byref(tuning) if tuning is not None else None, nrc.handle, target,
+                                             flags, C.byref(st)))
         return out, st
 
     def render_device(self, scene: Scene, cfg: IntegratorCfg, dev_ptr: int, tuning: Tuning | None = None,

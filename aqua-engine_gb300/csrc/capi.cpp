@@ -280,6 +280,7 @@ AQUA_API void aqua_destroy(aqua_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     workspace_release(ctx);
+    dev_free(ctx->nrc_ws.block);
     dev_free(ctx->trace_rays);
     dev_free(ctx->trace_hits);
     dev_free(ctx->trace_stats);
@@ -652,6 +653,19 @@ AQUA_API aqua_status aqua_nrc_forward(aqua_ctx* ctx, aqua_nrc* n, const uint16_t
         if (!(flags & AQUA_NRC_DEVICE_PTRS))
             AQ_CUDA(cudaMemcpyAsync(out, d_out, 12 * cnt, cudaMemcpyDeviceToHost, ctx->stream));
         AQ_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+AQUA_API aqua_status aqua_render_nrc(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg* cfg,
+                                     const aqua_tuning* tuning, aqua_nrc* nrc, float* rgb_out, uint32_t flags,
+                                     aqua_stats* stats) {
+    return guard(ctx, [&]() {
+        need(s && cfg && nrc && rgb_out, "scene, cfg, nrc and rgb_out must be non-NULL");
+        need_device(ctx);
+        aqua_tuning t;
+        if (tuning) t = *tuning;
+        else aqua_tuning_defaults(&t);
+        render_nrc(ctx, s, *cfg, t, nrc, rgb_out, flags, stats);
     });
 }
 

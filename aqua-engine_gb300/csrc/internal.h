@@ -80,6 +80,22 @@ struct NrcNet {
     float lr = 1e-2f, beta1 = 0.9f, beta2 = 0.99f, eps = 1e-8f;
     float bmin[3] = {0, 0, 0}, bext[3] = {1, 1, 1};
     uint64_t launches = 0;
+    double train_frac = 0.0;  // fraction of paths that train, adapted per frame
+};
+
+// Per-context buffers of a radiance-cache frame.
+struct NrcWorkspace {
+    DevBuf block;
+    size_t queries = 0, records = 0;  // capacities
+    float4* q_pix = nullptr;     // (pixel bits, throughput) per query
+    float* q_raw = nullptr;      // 16 raw features per query
+    uint16_t* q_x = nullptr;     // encoded queries (bf16 x 64)
+    float* q_pred = nullptr;     // cache output per query
+    float4* rec = nullptr;       // training-vertex records (6 words each)
+    float4* ltrain = nullptr;    // radiance per training path
+    float* t_raw = nullptr;      // permuted training features
+    uint16_t* t_x = nullptr;     // encoded training inputs
+    float* t_target = nullptr;   // training targets
 };
 
 enum { kCntQ0 = 0, kCntQ1 = 1, kCntShadow = 2, kCntBucket0 = 8 };
@@ -113,6 +129,7 @@ struct aqua_ctx {
     uint64_t alloc_count = 0;
     uint64_t fail_alloc_after = 0;
     aq::Workspace ws;
+    aq::NrcWorkspace nrc_ws;
     unsigned int* pinned_counter = nullptr;  // host-mapped copy of queue counts
     std::vector<cudaEvent_t> events;         // pool for stage timing
     aq::DevBuf trace_rays, trace_hits;       // staging for host-pointer traces
@@ -137,6 +154,10 @@ void trace_rays(aqua_ctx* ctx, aqua_scene* s, const aqua_ray* rays, size_t n, aq
 void render_path(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg& cfg, const aqua_tuning& tune,
                  float* rgb_out, uint32_t flags, aqua_stats* stats);
 void workspace_release(aqua_ctx* ctx);
+// One frame of the cached renderer (render.cu): wavefront with cache
+// queries and training paths, inference, online training.
+void render_nrc(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg& cfg, const aqua_tuning& tune,
+                aqua_nrc* nrc, float* rgb_out, uint32_t flags, aqua_stats* stats);
 
 // Radiance-cache network (nrc.cu).
 void nrc_alloc(aqua_ctx* ctx, NrcNet& net);

@@ -31,6 +31,12 @@ struct WaveParams {
     int32_t spp, spp_offset, max_depth, rr_depth;
     uint32_t slots, pixels;
     uint32_t nb;  // material buckets incl. the miss bucket (0 = unsorted)
+    // Radiance cache (NRC mode only).
+    int32_t query_depth;       // bounce at which non-training paths query the cache
+    uint32_t train_thresh;     // path trains when its 24-bit hash < this
+    uint32_t max_train_paths;  // capacity of the per-training-path accumulators
+    uint32_t max_records;      // capacity of the training-vertex records
+    int32_t visualize;         // 1 = the image is the cache seen at the first hit
 };
 
 struct WavePtrs {
@@ -48,7 +54,15 @@ struct WavePtrs {
     float4* film;
     uint32_t* counters;
     unsigned long long* stats;
+    // Radiance cache (NRC mode only).
+    float4* q_pix;    // per query: (pixel bits, throughput rgb)
+    float* q_raw;     // per query: 16 raw vertex features
+    float4* rec;      // per training vertex: 6 words (raw 16, throughput 3, radiance-before 3, path id)
+    float4* ltrain;   // per training path: radiance gathered so far
 };
+
+// Counters of the cache mode (after the material buckets).
+enum { kCntQuery = 3, kCntRecord = 4, kCntTrainPath = 5 };
 
 // ---------------------------------------------------------------- helpers
 __device__ __forceinline__ v3 f3(float4 a) { return mk(a.x, a.y, a.z); }
@@ -90,7 +104,10 @@ __device__ __forceinline__ void camera_ray(const DevCamera& c, uint32_t pixel, f
 
 __device__ __forceinline__ float draw(uint64_t& st, uint64_t inc) { return u01(pcg32_next(st, inc)); }
 
-// Starts work item j of slot s (pixel, sample), writing its camera ray.
+// Starts work item j of slot s (pixel, sample), writing its camera ray. The
+// path state's last word is depth (bits 0..7) | (training path id + 1) << 8;
+// the id is 0 outside the cache mode.
+template <bool NRC = false>
 __device__ __forceinline__ bool start_path(const DevScene& S, const WaveParams& P, const WavePtrs& W,
                                            uint32_t s, uint32_t j) {
     if (j >= slot_work(P, s)) return false;
@@ -103,7 +120,20 @@ __device__ __forceinline__ bool start_path(const DevScene& S, const WaveParams& 
     W.ray_o[s] = make_float4(o.x, o.y, o.z, 0.0f);
     W.ray_d[s] = make_float4(d.x, d.y, d.z, INFINITY);
     W.tp[s] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-    W.pst[s] = make_uint4((uint32_t)st, (uint32_t)(st >> 32), j, 0u);
+    uint32_t tag = 0;
+    if (NRC) {
+        // Training paths: a seeded hash of (pixel, sample) picks about the
+        // fraction the host asked for; they trace unbiased full paths.
+        uint32_t h = (uint32_t)(splitmix64(P.seed * 0x9E3779B97F4A7C15ULL ^ ((uint64_t)pixel << 24) ^ sample) >> 40);
+        if (h < P.train_thresh) {
+            uint32_t id = atomicAdd(&W.counters[kCntTrainPath], 1u);
+            if (id < P.max_train_paths) {
+                W.ltrain[id] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                tag = (id + 1u) << 8;
+            }
+        }
+    }
+    W.pst[s] = make_uint4((uint32_t)st, (uint32_t)(st >> 32), j, tag);
     return true;
 }
 
@@ -146,6 +176,7 @@ __device__ __forceinline__ void film_add(float4* film, uint32_t pixel, v3 c) {
 }
 
 // ---------------------------------------------------------------- kernels
+template <bool NRC = false>
 __global__ void k_raygen(DevScene S, WaveParams P, WavePtrs W) {
     uint32_t n = min(P.slots, P.pixels);
     uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -155,9 +186,26 @@ __global__ void k_raygen(DevScene S, WaveParams P, WavePtrs W) {
         W.counters[kCntShadow] = 0;
     }
     for (uint32_t s = tid; s < n; s += gridDim.x * blockDim.x) {
-        start_path(S, P, W, s, 0);
+        start_path<NRC>(S, P, W, s, 0);
         W.q_in[s] = s;
     }
+}
+
+// Raw cache features of a shading point (position, outgoing direction,
+// normal, roughness, diffuse albedo, specular F0).
+__device__ __forceinline__ void nrc_raw(float* o, v3 p, v3 wo, v3 n, float rough, v3 kd, v3 ks) {
+    o[0] = p.x; o[1] = p.y; o[2] = p.z;
+    o[3] = wo.x; o[4] = wo.y; o[5] = wo.z;
+    o[6] = n.x; o[7] = n.y; o[8] = n.z;
+    o[9] = rough;
+    o[10] = kd.x; o[11] = kd.y; o[12] = kd.z;
+    o[13] = ks.x; o[14] = ks.y; o[15] = ks.z;
+}
+
+__device__ __forceinline__ void ltrain_add(float4* L, uint32_t id, v3 c) {
+    float4 v = L[id];
+    v.x += c.x; v.y += c.y; v.z += c.z;
+    L[id] = v;
 }
 
 template <bool SORTED, bool COUNT>
@@ -199,7 +247,12 @@ __global__ void __launch_bounds__(128) k_trace_ext(DevScene S, WaveParams P, Wav
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&W.stats[kStatExt], (unsigned long long)n);
 }
 
-template <bool SORTED>
+// NRC: paths that are not training paths stop at bounce P.query_depth and
+// queue a cache query (pixel, throughput, raw features); training paths run
+// on and record every bounce (raw features, throughput, radiance gathered
+// so far) so that the radiance leaving each of their vertices becomes a
+// training target once the path is complete.
+template <bool SORTED, bool NRC = false>
 __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtrs W, uint32_t cnt_in,
                                                uint32_t cnt_out) {
     __shared__ float lut[256];
@@ -242,7 +295,8 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtr
         uint4 ps = W.pst[s];
         float4 tpv = W.tp[s];
         float4 h = W.hit[s];
-        uint32_t j = ps.z, depth = ps.w;
+        uint32_t j = ps.z, depth = ps.w & 0xffu, tag = ps.w & ~0xffu;
+        const uint32_t train_id = (tag >> 8) - 1u;  // valid when tag != 0
         uint32_t pixel = s + (j / (uint32_t)P.spp) * P.slots;
         uint64_t st = (uint64_t)ps.x | ((uint64_t)ps.y << 32), inc = pixel_inc(pixel);
         v3 thr = f3(tpv);
@@ -273,7 +327,8 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtr
                         float pl = L.e2.w * h.x * h.x / (L.e1.w * cos_l);
                         w = power_heuristic(pdf_b, pl);
                     }
-                    film_add(W.film, pixel, thr * f3(L.le) * w);
+                    if (!(NRC && P.visualize)) film_add(W.film, pixel, thr * f3(L.le) * w);
+                    if (NRC && tag) ltrain_add(W.ltrain, train_id, thr * f3(L.le) * w);
                 }
             }
             if ((int)depth < P.max_depth) {
@@ -290,14 +345,39 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtr
                     base = base * tex_bilinear(S, ti, tu, tv, lut);
                 }
                 Bsdf B = make_bsdf(base, m.b.x, m.b.y, m.b.z);
+                bool queried = false;
+                if (NRC) {
+                    v3 kd = base * (1.0f - m.b.x);
+                    if (!tag && (int)depth == P.query_depth) {
+                        uint32_t k = warp_append(&W.counters[kCntQuery], true);
+                        W.q_pix[k] = make_float4(__int_as_float((int)pixel), thr.x, thr.y, thr.z);
+                        nrc_raw(W.q_raw + 16 * (size_t)k, p, wo, ng, m.b.y, kd, B.F0);
+                        queried = true;
+                    } else if (tag) {
+                        uint32_t k = atomicAdd(&W.counters[kCntRecord], 1u);
+                        if (k < P.max_records) {
+                            float r[24];
+                            nrc_raw(r, p, wo, ng, m.b.y, kd, B.F0);
+                            float4 lb = W.ltrain[train_id];
+                            r[16] = thr.x; r[17] = thr.y; r[18] = thr.z;
+                            r[19] = lb.x; r[20] = lb.y; r[21] = lb.z;
+                            r[22] = __int_as_float((int)train_id);
+                            r[23] = 0.0f;
+                            float4* dst = W.rec + 6 * (size_t)k;
+#pragma unroll
+                            for (int q = 0; q < 6; ++q)
+                                dst[q] = make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+                        }
+                    }
+                }
                 v3 T, Bt;
                 onb(ng, T, Bt);
                 v3 wol = mk(dot(wo, T), dot(wo, Bt), dot(wo, ng));
                 float u[kBounceDims];
 #pragma unroll
-                for (int k = 0; k < kBounceDims; ++k) u[k] = draw(st, inc);
+                for (int k = 0; k < kBounceDims; ++k) u[k] = queried ? 0.0f : draw(st, inc);
                 // Next-event estimation: one light, one point, one shadow ray.
-                if (S.n_lights > 0 && wol.z > 0.0f) {
+                if (!queried && S.n_lights > 0 && wol.z > 0.0f) {
                     DevLight L = S.lights[pick_light(S, u[0])];
                     int ty = __float_as_int(L.p0.w);
                     float pmf = L.e2.w;
@@ -340,12 +420,13 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtr
                         v3 so = offset_ray(p, ng);
                         W.sh_o[k] = make_float4(so.x, so.y, so.z, __int_as_float((int)pixel));
                         W.sh_d[k] = make_float4(wi.x, wi.y, wi.z, dist * (1.0f - 1e-4f));
-                        W.sh_c[k] = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
+                        W.sh_c[k] = make_float4(contrib.x, contrib.y, contrib.z,
+                                                __int_as_float(NRC && tag ? (int)(train_id + 1u) : 0));
                     }
                 }
                 // BSDF sampling.
                 v3 wil = bsdf_sample(B, wol, u[3], u[4], u[5]);
-                if (wil.z > 0.0f && wol.z > 0.0f) {
+                if (!queried && wil.z > 0.0f && wol.z > 0.0f) {
                     float pdf = bsdf_pdf(B, wol, wil);
                     v3 f = bsdf_eval(B, wol, wil);
                     if (pdf > 0.0f) {
@@ -362,7 +443,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtr
                             W.ray_o[s] = make_float4(no.x, no.y, no.z, 0.0f);
                             W.ray_d[s] = make_float4(wi.x, wi.y, wi.z, INFINITY);
                             W.tp[s] = make_float4(thr.x, thr.y, thr.z, pdf);
-                            W.pst[s] = make_uint4((uint32_t)st, (uint32_t)(st >> 32), j, depth + 1);
+                            W.pst[s] = make_uint4((uint32_t)st, (uint32_t)(st >> 32), j, (depth + 1) | tag);
                             cont = true;
                         }
                     }
@@ -371,7 +452,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtr
         }
         if (!cont) {
             ++done_paths;
-            cont = start_path(S, P, W, s, j + 1);
+            cont = start_path<NRC>(S, P, W, s, j + 1);
         }
         uint32_t k = warp_append(out_cnt, cont);
         if (cont) W.q_out[k] = s;
@@ -380,7 +461,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtr
     if ((threadIdx.x & 31) == 0 && done_paths) atomicAdd(&W.stats[kStatPaths], done_paths);
 }
 
-template <bool COUNT>
+template <bool COUNT, bool NRC = false>
 __global__ void __launch_bounds__(128) k_shadow(DevScene S, WaveParams P, WavePtrs W) {
     uint32_t n = W.counters[kCntShadow];
     if (blockIdx.x == 0)
@@ -391,7 +472,11 @@ __global__ void __launch_bounds__(128) k_shadow(DevScene S, WaveParams P, WavePt
         TraceResult r = traverse<true, COUNT>(S, f3(o), f3(d), 0.0f, d.w, nodes, tris);
         if (r.tri < 0) {
             float4 c = W.sh_c[i];
-            film_add(W.film, (uint32_t)__float_as_int(o.w), mk(c.x, c.y, c.z));
+            if (!(NRC && P.visualize)) film_add(W.film, (uint32_t)__float_as_int(o.w), mk(c.x, c.y, c.z));
+            if (NRC) {
+                int id = __float_as_int(c.w);
+                if (id > 0) ltrain_add(W.ltrain, (uint32_t)(id - 1), mk(c.x, c.y, c.z));
+            }
         }
     }
     if (COUNT) {
@@ -654,6 +739,267 @@ void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, 
             stats->shade_ms = ts.total_ms();
             stats->shadow_ms = tsh.total_ms();
         }
+    }
+}
+
+// ---------------------------------------------------------------- radiance cache frame
+// film[pixel] += throughput * max(cache(x), 0) for every queued query. Several
+// samples of one pixel may have queried, so the add is atomic.
+__global__ void k_nrc_resolve(const float4* __restrict__ q_pix, const float* __restrict__ pred, uint32_t n,
+                              float4* film) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 q = q_pix[i];
+        uint32_t pixel = (uint32_t)__float_as_int(q.x);
+        float* f = reinterpret_cast<float*>(film + pixel);
+        atomicAdd(f + 0, q.y * fmaxf(pred[3 * (size_t)i + 0], 0.0f));
+        atomicAdd(f + 1, q.z * fmaxf(pred[3 * (size_t)i + 1], 0.0f));
+        atomicAdd(f + 2, q.w * fmaxf(pred[3 * (size_t)i + 2], 0.0f));
+    }
+}
+
+// Training targets: radiance leaving each recorded vertex toward its
+// predecessor = (radiance of the whole path - radiance gathered before the
+// vertex reflected anything) / throughput at the vertex, per channel.
+// Records are scattered by i -> (a*i + b) mod n so that consecutive
+// training batches mix paths, bounces and materials.
+constexpr float kNrcMinThroughput = 1e-3f;
+constexpr float kNrcMaxTarget = 1e3f;
+
+__global__ void k_nrc_targets(const float4* __restrict__ rec, uint32_t n, const float4* __restrict__ ltrain,
+                              uint64_t a, uint64_t b, float* __restrict__ raw_out, float* __restrict__ t_out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4* r = rec + 6 * (size_t)i;
+        uint32_t j = (uint32_t)((a * (uint64_t)i + b) % (uint64_t)n);
+        float4* ro = reinterpret_cast<float4*>(raw_out + 16 * (size_t)j);
+        ro[0] = r[0]; ro[1] = r[1]; ro[2] = r[2]; ro[3] = r[3];
+        float4 w4 = r[4], w5 = r[5];
+        // w4 = (beta.xyz, L_before.x), w5 = (L_before.yz, id, 0)
+        uint32_t id = (uint32_t)__float_as_int(w5.z);
+        float4 L = ltrain[id];
+        float t0 = fmaxf(L.x - w4.w, 0.0f) / fmaxf(w4.x, kNrcMinThroughput);
+        float t1 = fmaxf(L.y - w5.x, 0.0f) / fmaxf(w4.y, kNrcMinThroughput);
+        float t2 = fmaxf(L.z - w5.y, 0.0f) / fmaxf(w4.z, kNrcMinThroughput);
+        t_out[3 * (size_t)j + 0] = fminf(t0, kNrcMaxTarget);
+        t_out[3 * (size_t)j + 1] = fminf(t1, kNrcMaxTarget);
+        t_out[3 * (size_t)j + 2] = fminf(t2, kNrcMaxTarget);
+    }
+}
+
+static void ensure_nrc_workspace(aqua_ctx* ctx, size_t queries, size_t records) {
+    NrcWorkspace& w = ctx->nrc_ws;
+    if (w.block.ptr && w.queries >= queries && w.records >= records) return;
+    queries = std::max(queries, w.queries);
+    records = std::max(records, w.records);
+    dev_free(w.block);
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
+    size_t o_qp = take(16 * queries), o_qr = take(64 * queries), o_qx = take(128 * queries),
+           o_qo = take(12 * queries), o_rec = take(96 * records), o_lt = take(16 * records),
+           o_tr = take(64 * records), o_tx = take(128 * records), o_tt = take(12 * records);
+    dev_alloc(ctx, w.block, off);
+    char* b = (char*)w.block.ptr;
+    w.q_pix = (float4*)(b + o_qp);
+    w.q_raw = (float*)(b + o_qr);
+    w.q_x = (uint16_t*)(b + o_qx);
+    w.q_pred = (float*)(b + o_qo);
+    w.rec = (float4*)(b + o_rec);
+    w.ltrain = (float4*)(b + o_lt);
+    w.t_raw = (float*)(b + o_tr);
+    w.t_x = (uint16_t*)(b + o_tx);
+    w.t_target = (float*)(b + o_tt);
+    w.queries = queries;
+    w.records = records;
+}
+
+static uint64_t gcd64(uint64_t a, uint64_t b) {
+    while (b) { uint64_t t = a % b; a = b; b = t; }
+    return a;
+}
+
+void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, const aqua_tuning& tune,
+                aqua_nrc* nrc, float* rgb_out, uint32_t flags, aqua_stats* stats) {
+    const DevScene& S = sc->ds;
+    NrcNet& net = nrc->net;
+    if (cfg.spp <= 0) throw Error(AQUA_ERR_INVALID_ARG, "spp must be positive");
+    if (cfg.max_depth < 0 || cfg.max_depth > 250) throw Error(AQUA_ERR_INVALID_ARG, "max_depth must be in [0, 250]");
+    if (cfg.nrc_train_samples < 0) throw Error(AQUA_ERR_INVALID_ARG, "nrc_train_samples must be >= 0");
+    if (cfg.batch_size <= 0) throw Error(AQUA_ERR_INVALID_ARG, "batch_size must be positive");
+    size_t pixels = (size_t)S.cam.width * (size_t)S.cam.height;
+    if (pixels == 0 || pixels > (1u << 27)) throw Error(AQUA_ERR_INVALID_ARG, "resolution out of range");
+    size_t slots = tune.slots > 0 ? (size_t)tune.slots : std::min<size_t>(pixels, (size_t)1 << 21);
+    slots = std::min(slots, pixels);
+    if ((uint64_t)cfg.spp * ((pixels + slots - 1) / slots) > 0xFFFFFFFFull)
+        throw Error(AQUA_ERR_INVALID_ARG, "spp x pixels per slot exceeds 2^32");
+    if ((uint64_t)pixels * (uint64_t)cfg.spp > ((uint64_t)1 << 31))
+        throw Error(AQUA_ERR_INVALID_ARG, "one cache frame is limited to 2^31 samples");
+    bool sorted = tune.sort_by_material > 0 && S.n_mats + 1 <= 256;
+    size_t nb = sorted ? (size_t)S.n_mats + 1 : 0;
+    ensure_workspace(ctx, slots, nb, pixels);
+    size_t cap_q = pixels * (size_t)cfg.spp;
+    size_t cap_r = std::max<size_t>((size_t)cfg.nrc_train_samples, 1);
+    ensure_nrc_workspace(ctx, cap_q, cap_r);
+    Workspace& w = ctx->ws;
+    NrcWorkspace& nw = ctx->nrc_ws;
+    cudaStream_t st = ctx->stream;
+
+    // Positions are encoded relative to the scene's bounding box.
+    {
+        const float* n0 = sc->bvh.nodes.data();
+        float lo[3] = {std::min(n0[0], n0[4]), std::min(n0[2], n0[6]), std::min(n0[8], n0[10])};
+        float hi[3] = {std::max(n0[1], n0[5]), std::max(n0[3], n0[7]), std::max(n0[9], n0[11])};
+        for (int k = 0; k < 3; ++k) {
+            net.bmin[k] = lo[k];
+            net.bext[k] = std::max(hi[k] - lo[k], 1e-6f);
+        }
+    }
+    const bool visualize = cfg.visualize_cache != 0;
+    WaveParams P{};
+    P.seed = cfg.seed;
+    P.spp = cfg.spp;
+    P.spp_offset = cfg.spp_offset;
+    P.max_depth = cfg.max_depth;
+    P.rr_depth = cfg.rr_depth;
+    P.slots = (uint32_t)slots;
+    P.pixels = (uint32_t)pixels;
+    P.nb = (uint32_t)nb;
+    P.query_depth = visualize ? 0 : std::max(0, cfg.nrc_query_vertex - 1);
+    // Fraction of paths that train: aimed at nrc_train_samples records per
+    // frame (first frame: assume 3 recorded vertices per training path).
+    double frac = 0.0;
+    if (!visualize && cfg.nrc_train_samples > 0)
+        frac = net.train_frac > 0.0 ? net.train_frac
+                                    : (double)cfg.nrc_train_samples / (3.0 * (double)pixels * cfg.spp);
+    frac = std::min(frac, 1.0);
+    P.train_thresh = (uint32_t)std::min(16777216.0, frac * 16777216.0);
+    P.max_train_paths = (uint32_t)cap_r;
+    P.max_records = (uint32_t)cap_r;
+    P.visualize = visualize ? 1 : 0;
+    WavePtrs W{};
+    W.ray_o = w.ray_o; W.ray_d = w.ray_d; W.hit = w.hit; W.tp = w.tp; W.pst = w.pst;
+    W.bucket = w.bucket; W.sh_o = w.sh_o; W.sh_d = w.sh_d; W.sh_c = w.sh_c; W.film = w.film;
+    W.counters = w.counters; W.stats = w.stats;
+    W.q_pix = nw.q_pix; W.q_raw = nw.q_raw; W.rec = nw.rec; W.ltrain = nw.ltrain;
+
+    auto trace_k = sorted ? k_trace_ext<true, false> : k_trace_ext<false, false>;
+    auto shade_k = sorted ? k_shade<true, true> : k_shade<false, true>;
+    auto shadow_k = k_shadow<false, true>;
+    int g_trace = grid_for(ctx, trace_k, 128, tune.blocks_per_sm);
+    int g_shade = grid_for(ctx, shade_k, 128, tune.blocks_per_sm);
+    int g_shadow = grid_for(ctx, shadow_k, 128, tune.blocks_per_sm);
+
+    cudaEvent_t ev[4];
+    size_t next_event = 0;
+    StageTimer tm{ctx, true, {}, &next_event};
+    for (auto& e : ev) e = tm.get();
+    AQ_CUDA(cudaMemsetAsync(w.film, 0, 16 * pixels, st));
+    AQ_CUDA(cudaMemsetAsync(w.stats, 0, 8 * 16, st));
+    AQ_CUDA(cudaMemsetAsync(w.counters, 0, 4 * (kCntBucket0 + std::max<size_t>(nb, 1)), st));
+    AQ_CUDA(cudaEventRecord(ev[0], st));
+    uint64_t launches = 0;
+    W.q_in = w.q[0];
+    W.q_out = w.q[1];
+    {
+        int g = (int)std::min<size_t>((slots + 255) / 256, (size_t)ctx->num_sms * 16);
+        k_raygen<true><<<std::max(g, 1), 256, 0, st>>>(S, P, W);
+        AQ_CUDA(cudaGetLastError());
+        ++launches;
+    }
+    const int chunk = tune.iters_per_graph > 0 ? tune.iters_per_graph : 16;
+    const uint64_t max_iters =
+        (uint64_t)(cfg.max_depth + 2) * (uint64_t)cfg.spp * ((pixels + slots - 1) / slots) + 64;
+    uint64_t iter = 0;
+    unsigned int* pc = ctx->pinned_counter;
+    while (true) {
+        for (int k = 0; k < chunk; ++k, ++iter) {
+            uint32_t in = (uint32_t)(iter & 1), out = 1u - in;
+            W.q_in = w.q[in];
+            W.q_out = w.q[out];
+            trace_k<<<g_trace, 128, 0, st>>>(S, P, W, in, out);
+            shade_k<<<g_shade, 128, 0, st>>>(S, P, W, in, out);
+            shadow_k<<<g_shadow, 128, 0, st>>>(S, P, W);
+            launches += 3;
+        }
+        AQ_CUDA(cudaGetLastError());
+        AQ_CUDA(cudaMemcpyAsync(&pc[8], &w.counters[iter & 1], 4, cudaMemcpyDeviceToHost, st));
+        AQ_CUDA(cudaMemcpyAsync(&pc[9], &w.counters[kCntQuery], 12, cudaMemcpyDeviceToHost, st));
+        AQ_CUDA(cudaStreamSynchronize(st));
+        if (pc[8] == 0) break;
+        if (iter > max_iters) throw Error(AQUA_ERR_TIMEOUT, "wavefront did not drain within the iteration bound");
+    }
+    AQ_CUDA(cudaEventRecord(ev[1], st));
+    const uint32_t nq = pc[9], nrec = std::min(pc[10], P.max_records), ntp = pc[11];
+    // Cache queries: encode, infer, add throughput x prediction.
+    if (nq > 0) {
+        nrc_encode_dev(ctx, net, nw.q_raw, (int)nq, nw.q_x);
+        nrc_forward_dev(ctx, net, nw.q_x, (int)nq, nw.q_pred);
+        int g = (int)std::min<size_t>((nq + 255) / 256, (size_t)ctx->num_sms * 16);
+        k_nrc_resolve<<<g, 256, 0, st>>>(nw.q_pix, nw.q_pred, nq, w.film);
+        AQ_CUDA(cudaGetLastError());
+        launches += 3;
+    }
+    AQ_CUDA(cudaEventRecord(ev[2], st));
+    // Online training on this frame's records.
+    double loss = 0.0;
+    int steps = 0;
+    if (nrec > 0 && !visualize) {
+        uint64_t a = 2654435761ull % nrec, b = 0x9E37ull % nrec;
+        if (a == 0) a = 1;
+        while (gcd64(a, nrec) != 1) ++a;
+        int g = (int)std::min<size_t>((nrec + 255) / 256, (size_t)ctx->num_sms * 16);
+        k_nrc_targets<<<g, 256, 0, st>>>(nw.rec, nrec, nw.ltrain, a, b, nw.t_raw, nw.t_target);
+        AQ_CUDA(cudaGetLastError());
+        nrc_encode_dev(ctx, net, nw.t_raw, (int)nrec, nw.t_x);
+        launches += 2;
+        int batch = cfg.batch_size;
+        steps = (int)((nrec + (uint32_t)batch - 1) / (uint32_t)batch);
+        if (cfg.training_iters > 0) steps = std::min(steps, cfg.training_iters);
+        for (int sidx = 0; sidx < steps; ++sidx) {
+            size_t r0 = (size_t)sidx * (size_t)batch;
+            int rows = (int)std::min<size_t>((size_t)batch, nrec - r0);
+            nrc_train_step_dev(ctx, net, nw.t_x + 64 * r0, nw.t_target + 3 * r0, rows);
+            launches += 5;
+        }
+        AQ_CUDA(cudaMemcpyAsync(&loss, net.loss, 8, cudaMemcpyDeviceToHost, st));
+        // Aim the next frame's training-path fraction at the record budget.
+        double per_path = ntp > 0 ? (double)pc[10] / (double)std::min<uint32_t>(ntp, P.max_train_paths) : 3.0;
+        double want = (double)cfg.nrc_train_samples / std::max(per_path, 1.0);
+        net.train_frac = std::min(1.0, want / ((double)pixels * cfg.spp));
+    }
+    AQ_CUDA(cudaEventRecord(ev[3], st));
+    float* dst = (flags & AQUA_RENDER_DEVICE_FILM) ? rgb_out : w.out_rgb;
+    bool acc = (flags & AQUA_RENDER_ACCUMULATE) != 0;
+    if (acc && !(flags & AQUA_RENDER_DEVICE_FILM))
+        AQ_CUDA(cudaMemcpyAsync(dst, rgb_out, 12 * pixels, cudaMemcpyHostToDevice, st));
+    {
+        int g = (int)std::min<size_t>((pixels + 255) / 256, (size_t)ctx->num_sms * 16);
+        k_resolve<<<g, 256, 0, st>>>(w.film, dst, (uint32_t)pixels, 1.0f / (float)cfg.spp, acc ? 1 : 0);
+        AQ_CUDA(cudaGetLastError());
+        ++launches;
+    }
+    if (!(flags & AQUA_RENDER_DEVICE_FILM))
+        AQ_CUDA(cudaMemcpyAsync(rgb_out, w.out_rgb, 12 * pixels, cudaMemcpyDeviceToHost, st));
+    unsigned long long hs[16];
+    AQ_CUDA(cudaMemcpyAsync(hs, w.stats, 8 * 16, cudaMemcpyDeviceToHost, st));
+    AQ_CUDA(cudaStreamSynchronize(st));
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        float ms = 0.0f, q_ms = 0.0f, t_ms = 0.0f;
+        AQ_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[3]));
+        AQ_CUDA(cudaEventElapsedTime(&q_ms, ev[1], ev[2]));
+        AQ_CUDA(cudaEventElapsedTime(&t_ms, ev[2], ev[3]));
+        stats->device_ms = ms;
+        stats->nrc_ms = q_ms + t_ms;
+        stats->paths = hs[kStatPaths];
+        stats->ext_rays = hs[kStatExt];
+        stats->shadow_rays = hs[kStatShadow];
+        stats->iterations = iter;
+        stats->trace_launches = stats->shade_launches = stats->shadow_launches = iter;
+        stats->total_launches = launches;
+        stats->nrc_queries = nq;
+        stats->nrc_train_records = nrec;
+        stats->nrc_loss = nrec > 0 && steps > 0 ? loss / (double)(std::min<size_t>((size_t)cfg.batch_size,
+                                                                                  nrec - (size_t)(steps - 1) * cfg.batch_size) * 3)
+                                                : 0.0;
     }
 }
 

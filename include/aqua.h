@@ -341,6 +341,20 @@ AQUA_API aqua_status aqua_nrc_forward(aqua_ctx* ctx, aqua_nrc* nrc, const uint16
 AQUA_API aqua_status aqua_nrc_train_step(aqua_ctx* ctx, aqua_nrc* nrc, const uint16_t* x, const float* target,
                                          size_t n, double* loss, uint32_t flags);
 
+/* One frame of the cached renderer (`"type": "nrc"`, integrator.json:2).
+ * cfg->spp samples per pixel. Paths stop at vertex cfg->nrc_query_vertex
+ * (vertex 1 = first hit) and add throughput x cache; about
+ * cfg->nrc_train_samples vertices of unbiased training paths become
+ * training records, and the network takes ceil(records / cfg->batch_size)
+ * Adam steps (at most cfg->training_iters when that is > 0) after the frame
+ * is rendered. Positions are encoded relative to the scene's bounding box.
+ * cfg->visualize_cache renders the cache at the first hit instead (no
+ * training). Same rgb_out, flags and stats as aqua_render; the stats'
+ * nrc_* fields are filled. */
+AQUA_API aqua_status aqua_render_nrc(aqua_ctx* ctx, aqua_scene* scene, const aqua_integrator_cfg* cfg,
+                                     const aqua_tuning* tuning, aqua_nrc* nrc, float* rgb_out, uint32_t flags,
+                                     aqua_stats* stats);
+
 /* aqua_render without any device allocation. No counterpart in the
  * reference: it exists for callers that may not let a library call
  * cudaMalloc — engines that hand out all device memory from their own arena

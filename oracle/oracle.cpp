@@ -469,9 +469,18 @@ Closest<double> closest<double>(const orc_scene* s, V3<double> o, V3<double> d, 
     return {h.id >= 0, h.t, h.u, h.v, h.id};
 }
 
+// Optional constant radiance cache: paths stop at bounce query_depth and
+// add throughput x cache_rgb (the device's cache query with a network whose
+// output is that constant).
+struct CacheConst {
+    int query_depth = -1;
+    double rgb[3] = {0, 0, 0};
+};
+
 template <class T>
 void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>& cdf, int32_t spp, int32_t spp_offset,
-                  int32_t max_depth, int32_t rr_depth, uint64_t seed, uint32_t pixel, double sum[3], double st[3]) {
+                  int32_t max_depth, int32_t rr_depth, uint64_t seed, uint32_t pixel, double sum[3], double st[3],
+                  const CacheConst& cache = CacheConst()) {
     const aqua_camera& c = s->cam;
     T tan_half = (T)std::tan(0.5 * (double)c.fov_deg * M_PI / 180.0);
     T aspect = (T)c.width / (T)c.height;
@@ -531,6 +540,10 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
                 }
             }
             if (depth >= max_depth) break;
+            if (depth == cache.query_depth) {
+                for (int c2 = 0; c2 < 3; ++c2) sum[c2] += (double)at(thr, c2) * cache.rgb[c2];
+                break;
+            }
             if (dot3(ng, wo) < T(0)) ng = -ng;
             const aqua_material& m = s->mats[s->tri_mat[h.id]];
             V3<T> base{(T)m.base_color[0], (T)m.base_color[1], (T)m.base_color[2]};
@@ -780,6 +793,13 @@ void orc_nrc_encode(const float* raw, int64_t n, const float* bmin, const float*
 
 double orc_srgb_to_linear(double c) { return c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4); }
 
+int orc_render(const orc_scene* s, int precision, int32_t spp, int32_t spp_offset, int32_t max_depth,
+               int32_t rr_depth, uint64_t seed, int threads, int64_t pixel_begin, int64_t pixel_end, float* out,
+               double* stats) {
+    return orc_render_cached(s, precision, spp, spp_offset, max_depth, rr_depth, seed, threads, pixel_begin,
+                             pixel_end, -1, nullptr, out, stats);
+}
+
 uint32_t orc_pcg32_first(uint64_t initstate, uint64_t initseq, uint32_t* out, int n) {
     Pcg r;
     r.seed(initstate, initseq);
@@ -847,10 +867,14 @@ void orc_trace_brute_f64(const orc_scene* s, const float* rays, int64_t n, doubl
     });
 }
 
-int orc_render(const orc_scene* s, int precision, int32_t spp, int32_t spp_offset, int32_t max_depth,
-               int32_t rr_depth, uint64_t seed, int threads, int64_t pixel_begin, int64_t pixel_end, float* out,
-               double* stats) {
+int orc_render_cached(const orc_scene* s, int precision, int32_t spp, int32_t spp_offset, int32_t max_depth,
+                      int32_t rr_depth, uint64_t seed, int threads, int64_t pixel_begin, int64_t pixel_end,
+                      int32_t query_depth, const float* cache_rgb, float* out, double* stats) {
     if (!s || !out || spp <= 0 || (precision != 32 && precision != 64)) return 1;
+    CacheConst cache;
+    cache.query_depth = cache_rgb ? query_depth : -1;
+    if (cache_rgb)
+        for (int c = 0; c < 3; ++c) cache.rgb[c] = cache_rgb[c];
     int64_t npix = (int64_t)s->cam.width * s->cam.height;
     pixel_begin = std::max<int64_t>(0, pixel_begin);
     pixel_end = std::min<int64_t>(npix, pixel_end);
@@ -871,9 +895,9 @@ int orc_render(const orc_scene* s, int precision, int32_t spp, int32_t spp_offse
         double sum[3] = {0, 0, 0};
         double* sk = &st[3 * (size_t)k];
         if (precision == 64)
-            render_pixel<double>(s, lut, cdf, spp, spp_offset, max_depth, rr_depth, seed, pixel, sum, sk);
+            render_pixel<double>(s, lut, cdf, spp, spp_offset, max_depth, rr_depth, seed, pixel, sum, sk, cache);
         else
-            render_pixel<float>(s, lut, cdf, spp, spp_offset, max_depth, rr_depth, seed, pixel, sum, sk);
+            render_pixel<float>(s, lut, cdf, spp, spp_offset, max_depth, rr_depth, seed, pixel, sum, sk, cache);
         for (int c = 0; c < 3; ++c) out[3 * (size_t)pixel + c] = (float)(sum[c] / spp);
     });
     if (stats) {

@@ -70,6 +70,12 @@ int orc_render(const orc_scene* s, int precision, int32_t spp, int32_t spp_offse
                int32_t rr_depth, uint64_t seed, int threads, int64_t pixel_begin, int64_t pixel_end,
                float* out, double* stats);
 
+/* As orc_render, with a constant radiance cache: every path stops at bounce
+ * query_depth (0 = first hit) and adds throughput x cache_rgb there. */
+int orc_render_cached(const orc_scene* s, int precision, int32_t spp, int32_t spp_offset, int32_t max_depth,
+                      int32_t rr_depth, uint64_t seed, int threads, int64_t pixel_begin, int64_t pixel_end,
+                      int32_t query_depth, const float* cache_rgb, float* out, double* stats);
+
 /* Radiance-cache network (64 -> 5 x 64 ReLU -> 3, no biases; weights FP32
  * row-major [out][in], W1..W5 then W6: 20,672 values), in double.
  * emulate_bf16 = 1 rounds weights, inputs, stored activations and stored

@@ -47,6 +47,9 @@ def lib():
         L.orc_render.argtypes = [P, C.c_int, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_int,
                                  C.c_int64, C.c_int64, P, P]
         L.orc_render.restype = C.c_int
+        L.orc_render_cached.argtypes = [P, C.c_int, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
+                                        C.c_int, C.c_int64, C.c_int64, C.c_int32, P, P, P]
+        L.orc_render_cached.restype = C.c_int
         L.orc_srgb_to_linear.argtypes = [C.c_double]
         L.orc_srgb_to_linear.restype = C.c_double
         L.orc_pcg32_first.argtypes = [C.c_uint64, C.c_uint64, P, C.c_int]
@@ -126,13 +129,16 @@ class OracleScene:
 
     # -- rendering ---------------------------------------------------------
     def render(self, spp: int, max_depth: int, seed: int = 0, precision: int = 64, rr_depth: int = 3,
-               spp_offset: int = 0, threads: int = 0, pixel_begin: int = 0, pixel_end: int | None = None):
+               spp_offset: int = 0, threads: int = 0, pixel_begin: int = 0, pixel_end: int | None = None,
+               query_depth: int = -1, cache_rgb=None):
         n = self.width * self.height
         out = np.zeros((self.height, self.width, 3), np.float32)
         stats = np.zeros(3, np.float64)
         pe = n if pixel_end is None else pixel_end
-        r = lib().orc_render(C.byref(self.s), precision, spp, spp_offset, max_depth, rr_depth, seed, threads,
-                             pixel_begin, pe, _p(out), _p(stats))
+        cache = None if cache_rgb is None else np.ascontiguousarray(cache_rgb, np.float32)
+        r = lib().orc_render_cached(C.byref(self.s), precision, spp, spp_offset, max_depth, rr_depth, seed,
+                                    threads, pixel_begin, pe, query_depth,
+                                    None if cache is None else _p(cache), _p(out), _p(stats))
         if r != 0:
             raise RuntimeError("orc_render rejected its arguments")
         return out, stats
