@@ -37,6 +37,10 @@ struct WaveParams {
     uint32_t max_train_paths;  // capacity of the per-training-path accumulators
     uint32_t max_records;      // capacity of the training-vertex records
     int32_t visualize;         // 1 = the image is the cache seen at the first hit
+    // Sample replicas (0 or 1 = off). With K > 1 there are K slots per pixel:
+    // slot s = r * pixels + p runs samples r, r + K, r + 2K, ... of pixel p
+    // into film copy r; the copies are summed in order r = 0..K-1.
+    uint32_t replicas;
 };
 
 struct WavePtrs {
@@ -68,9 +72,33 @@ enum { kCntQuery = 3, kCntRecord = 4, kCntTrainPath = 5 };
 __device__ __forceinline__ v3 f3(float4 a) { return mk(a.x, a.y, a.z); }
 
 __device__ __forceinline__ uint32_t slot_work(const WaveParams& P, uint32_t s) {
+    if (P.replicas > 1) {
+        uint32_t r = s / P.pixels;
+        return r < (uint32_t)P.spp ? ((uint32_t)P.spp - r + P.replicas - 1) / P.replicas : 0u;
+    }
     if (s >= P.pixels) return 0;
     uint32_t npix = (P.pixels - s + P.slots - 1) / P.slots;
     return npix * (uint32_t)P.spp;
+}
+
+// Pixel (the RNG stream), sample index and film entry of work item j of
+// slot s.
+struct PathId {
+    uint32_t pixel, sample, film;
+};
+__device__ __forceinline__ PathId path_id(const WaveParams& P, uint32_t s, uint32_t j) {
+    PathId id;
+    if (P.replicas > 1) {
+        uint32_t r = s / P.pixels;
+        id.pixel = s - r * P.pixels;
+        id.sample = (uint32_t)P.spp_offset + r + j * P.replicas;
+        id.film = s;
+    } else {
+        id.pixel = s + (j / (uint32_t)P.spp) * P.slots;
+        id.sample = (uint32_t)P.spp_offset + j % (uint32_t)P.spp;
+        id.film = id.pixel;
+    }
+    return id;
 }
 
 // Shirley-Chiu concentric square-to-disk mapping.
@@ -111,8 +139,8 @@ template <bool NRC = false>
 __device__ __forceinline__ bool start_path(const DevScene& S, const WaveParams& P, const WavePtrs& W,
                                            uint32_t s, uint32_t j) {
     if (j >= slot_work(P, s)) return false;
-    uint32_t pixel = s + (j / (uint32_t)P.spp) * P.slots;
-    uint32_t sample = (uint32_t)P.spp_offset + j % (uint32_t)P.spp;
+    PathId pid = path_id(P, s, j);
+    uint32_t pixel = pid.pixel, sample = pid.sample;
     uint64_t st = path_rng_state(P.seed, pixel, sample), inc = pixel_inc(pixel);
     float u0 = draw(st, inc), u1 = draw(st, inc), u2 = draw(st, inc), u3 = draw(st, inc);
     v3 o, d;
@@ -178,7 +206,7 @@ __device__ __forceinline__ void film_add(float4* film, uint32_t pixel, v3 c) {
 // ---------------------------------------------------------------- kernels
 template <bool NRC = false>
 __global__ void k_raygen(DevScene S, WaveParams P, WavePtrs W) {
-    uint32_t n = min(P.slots, P.pixels);
+    uint32_t n = P.replicas > 1 ? P.slots : min(P.slots, P.pixels);
     uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     if (tid == 0) {
         W.counters[kCntQ0] = n;
@@ -297,8 +325,9 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtr
         float4 h = W.hit[s];
         uint32_t j = ps.z, depth = ps.w & 0xffu, tag = ps.w & ~0xffu;
         const uint32_t train_id = (tag >> 8) - 1u;  // valid when tag != 0
-        uint32_t pixel = s + (j / (uint32_t)P.spp) * P.slots;
-        uint64_t st = (uint64_t)ps.x | ((uint64_t)ps.y << 32), inc = pixel_inc(pixel);
+        const PathId pid = path_id(P, s, j);
+        const uint32_t pixel = pid.film;  // film entry owned by this slot
+        uint64_t st = (uint64_t)ps.x | ((uint64_t)ps.y << 32), inc = pixel_inc(pid.pixel);
         v3 thr = f3(tpv);
         float pdf_b = tpv.w;
         int32_t tri = __float_as_int(h.w);
@@ -492,9 +521,16 @@ __global__ void __launch_bounds__(128) k_shadow(DevScene S, WaveParams P, WavePt
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&W.stats[kStatShadow], (unsigned long long)n);
 }
 
-__global__ void k_resolve(const float4* film, float* out, uint32_t pixels, float scale, int accumulate) {
+// out = film / spp (or out += film). With sample replicas the K film copies
+// are summed in replica order first.
+__global__ void k_resolve(const float4* film, float* out, uint32_t pixels, float scale, int accumulate,
+                          uint32_t replicas = 1) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < pixels; p += gridDim.x * blockDim.x) {
         float4 f = film[p];
+        for (uint32_t r = 1; r < replicas; ++r) {
+            float4 g = film[(size_t)r * pixels + p];
+            f.x += g.x; f.y += g.y; f.z += g.z;
+        }
         if (accumulate) {
             out[3 * (size_t)p + 0] += f.x;
             out[3 * (size_t)p + 1] += f.y;
@@ -591,29 +627,53 @@ struct StageTimer {
         return t;
     }
 };
+
+// Paths in flight: one slot per pixel up to 2^21 slots; below 2^20 pixels,
+// K sample replicas per pixel (K <= spp) so that about 2^20 paths are in
+// flight, enough to fill the GPU.
+struct SlotPlan {
+    size_t slots;
+    uint32_t replicas;
+};
+SlotPlan plan_slots(size_t pixels, int spp, const aqua_tuning& tune) {
+    const size_t target = (size_t)1 << 20;
+    size_t k = 1;
+    if (tune.replicas > 0) k = (size_t)tune.replicas;
+    else if (tune.slots <= 0 && pixels < target) k = (target + pixels - 1) / pixels;
+    k = std::max<size_t>(1, std::min<size_t>(k, (size_t)spp));
+    k = std::min<size_t>(k, ((size_t)1 << 24) / pixels + 1);
+    SlotPlan p;
+    if (k > 1) {
+        p.slots = k * pixels;
+        p.replicas = (uint32_t)k;
+    } else {
+        size_t slots = tune.slots > 0 ? (size_t)tune.slots : std::min<size_t>(pixels, (size_t)1 << 21);
+        p.slots = std::min(slots, pixels);
+        p.replicas = 1;
+        if ((uint64_t)spp * ((pixels + p.slots - 1) / p.slots) > 0xFFFFFFFFull)
+            throw Error(AQUA_ERR_INVALID_ARG, "spp x pixels per slot exceeds 2^32");
+    }
+    return p;
+}
 }  // namespace
 
 void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, const aqua_tuning& tune,
                  float* rgb_out, uint32_t flags, aqua_stats* stats) {
     const DevScene& S = sc->ds;
     if (cfg.spp <= 0) throw Error(AQUA_ERR_INVALID_ARG, "spp must be positive");
-    if (cfg.max_depth < 0) throw Error(AQUA_ERR_INVALID_ARG, "max_depth must be >= 0");
+    if (cfg.max_depth < 0 || cfg.max_depth > 250) throw Error(AQUA_ERR_INVALID_ARG, "max_depth must be in [0, 250]");
     size_t pixels = (size_t)S.cam.width * (size_t)S.cam.height;
     if (pixels == 0 || pixels > (1u << 27)) throw Error(AQUA_ERR_INVALID_ARG, "resolution out of range");
-    if ((uint64_t)cfg.spp * (pixels + 1) > 0xFFFFFFFFull && tune.slots > 0 &&
-        (uint64_t)cfg.spp * ((pixels + tune.slots - 1) / tune.slots) > 0xFFFFFFFFull)
-        throw Error(AQUA_ERR_INVALID_ARG, "spp x pixels per slot exceeds 2^32");
-    size_t slots = tune.slots > 0 ? (size_t)tune.slots : std::min<size_t>(pixels, (size_t)1 << 21);
-    slots = std::min(slots, pixels);
-    if ((uint64_t)cfg.spp * ((pixels + slots - 1) / slots) > 0xFFFFFFFFull)
-        throw Error(AQUA_ERR_INVALID_ARG, "spp x pixels per slot exceeds 2^32");
+    const SlotPlan plan = plan_slots(pixels, cfg.spp, tune);
+    const size_t slots = plan.slots;
     bool sorted = tune.sort_by_material > 0 && S.n_mats + 1 <= 256;
     size_t nb = sorted ? (size_t)S.n_mats + 1 : 0;
-    ensure_workspace(ctx, slots, nb, pixels);
+    ensure_workspace(ctx, slots, nb, pixels * plan.replicas);
     Workspace& w = ctx->ws;
     cudaStream_t st = ctx->stream;
 
-    WaveParams P;
+    WaveParams P{};
+    P.replicas = plan.replicas;
     P.seed = cfg.seed;
     P.spp = cfg.spp;
     P.spp_offset = cfg.spp_offset;
@@ -648,7 +708,7 @@ void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, 
     ev0 = tt.get();
     ev1 = tt.get();
 
-    AQ_CUDA(cudaMemsetAsync(w.film, 0, 16 * pixels, st));
+    AQ_CUDA(cudaMemsetAsync(w.film, 0, 16 * pixels * plan.replicas, st));
     AQ_CUDA(cudaMemsetAsync(w.stats, 0, 8 * 16, st));
     AQ_CUDA(cudaMemsetAsync(w.counters, 0, 4 * (kCntBucket0 + std::max<size_t>(nb, 1)), st));
     AQ_CUDA(cudaEventRecord(ev0, st));
@@ -656,7 +716,7 @@ void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, 
     W.q_in = w.q[0];
     W.q_out = w.q[1];
     {
-        int g = (int)std::min<size_t>((std::min(slots, pixels) + 255) / 256, (size_t)ctx->num_sms * 16);
+        int g = (int)std::min<size_t>((slots + 255) / 256, (size_t)ctx->num_sms * 16);
         k_raygen<<<std::max(g, 1), 256, 0, st>>>(S, P, W);
         AQ_CUDA(cudaGetLastError());
         ++launches;
@@ -706,7 +766,8 @@ void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, 
         AQ_CUDA(cudaMemcpyAsync(dst, rgb_out, 12 * pixels, cudaMemcpyHostToDevice, st));
     {
         int g = (int)std::min<size_t>((pixels + 255) / 256, (size_t)ctx->num_sms * 16);
-        k_resolve<<<g, 256, 0, st>>>(w.film, dst, (uint32_t)pixels, 1.0f / (float)cfg.spp, acc ? 1 : 0);
+        k_resolve<<<g, 256, 0, st>>>(w.film, dst, (uint32_t)pixels, 1.0f / (float)cfg.spp, acc ? 1 : 0,
+                                     plan.replicas);
         AQ_CUDA(cudaGetLastError());
         ++launches;
     }
@@ -826,15 +887,13 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     if (cfg.batch_size <= 0) throw Error(AQUA_ERR_INVALID_ARG, "batch_size must be positive");
     size_t pixels = (size_t)S.cam.width * (size_t)S.cam.height;
     if (pixels == 0 || pixels > (1u << 27)) throw Error(AQUA_ERR_INVALID_ARG, "resolution out of range");
-    size_t slots = tune.slots > 0 ? (size_t)tune.slots : std::min<size_t>(pixels, (size_t)1 << 21);
-    slots = std::min(slots, pixels);
-    if ((uint64_t)cfg.spp * ((pixels + slots - 1) / slots) > 0xFFFFFFFFull)
-        throw Error(AQUA_ERR_INVALID_ARG, "spp x pixels per slot exceeds 2^32");
+    const SlotPlan plan = plan_slots(pixels, cfg.spp, tune);
+    const size_t slots = plan.slots;
     if ((uint64_t)pixels * (uint64_t)cfg.spp > ((uint64_t)1 << 31))
         throw Error(AQUA_ERR_INVALID_ARG, "one cache frame is limited to 2^31 samples");
     bool sorted = tune.sort_by_material > 0 && S.n_mats + 1 <= 256;
     size_t nb = sorted ? (size_t)S.n_mats + 1 : 0;
-    ensure_workspace(ctx, slots, nb, pixels);
+    ensure_workspace(ctx, slots, nb, pixels * plan.replicas);
     size_t cap_q = pixels * (size_t)cfg.spp;
     size_t cap_r = std::max<size_t>((size_t)cfg.nrc_train_samples, 1);
     ensure_nrc_workspace(ctx, cap_q, cap_r);
@@ -854,6 +913,7 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     }
     const bool visualize = cfg.visualize_cache != 0;
     WaveParams P{};
+    P.replicas = plan.replicas;
     P.seed = cfg.seed;
     P.spp = cfg.spp;
     P.spp_offset = cfg.spp_offset;
@@ -891,7 +951,7 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     size_t next_event = 0;
     StageTimer tm{ctx, true, {}, &next_event};
     for (auto& e : ev) e = tm.get();
-    AQ_CUDA(cudaMemsetAsync(w.film, 0, 16 * pixels, st));
+    AQ_CUDA(cudaMemsetAsync(w.film, 0, 16 * pixels * plan.replicas, st));
     AQ_CUDA(cudaMemsetAsync(w.stats, 0, 8 * 16, st));
     AQ_CUDA(cudaMemsetAsync(w.counters, 0, 4 * (kCntBucket0 + std::max<size_t>(nb, 1)), st));
     AQ_CUDA(cudaEventRecord(ev[0], st));
@@ -972,7 +1032,8 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
         AQ_CUDA(cudaMemcpyAsync(dst, rgb_out, 12 * pixels, cudaMemcpyHostToDevice, st));
     {
         int g = (int)std::min<size_t>((pixels + 255) / 256, (size_t)ctx->num_sms * 16);
-        k_resolve<<<g, 256, 0, st>>>(w.film, dst, (uint32_t)pixels, 1.0f / (float)cfg.spp, acc ? 1 : 0);
+        k_resolve<<<g, 256, 0, st>>>(w.film, dst, (uint32_t)pixels, 1.0f / (float)cfg.spp, acc ? 1 : 0,
+                                     plan.replicas);
         AQ_CUDA(cudaGetLastError());
         ++launches;
     }
@@ -1075,7 +1136,7 @@ void render_noalloc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cf
     char* base = (char*)noalloc_base(ctx->device);
     cudaStream_t st = ctx->stream;
 
-    WaveParams P;
+    WaveParams P{};  // zero: no replicas, no cache mode
     P.seed = cfg.seed;
     P.spp = cfg.spp;
     P.spp_offset = cfg.spp_offset;

@@ -109,8 +109,9 @@ typedef struct aqua_integrator_cfg {
 } aqua_integrator_cfg;
 
 /* Launch shape of the wavefront. 0 in any field = the library default.
- * Every choice gives a bit-identical image: each pixel is owned by exactly one
- * path slot, which runs that pixel's samples in order. */
+ * For a given `replicas` value every choice gives a bit-identical image: each
+ * pixel (or, with replicas, each pixel's film copy) is owned by exactly one
+ * path slot, which runs its samples in order. */
 typedef struct aqua_tuning {
     int32_t slots;          /* paths in flight (0 = one per pixel, capped)   */
     int32_t block_trace;    /* threads per block, traversal kernels          */
@@ -118,8 +119,10 @@ typedef struct aqua_tuning {
     int32_t sort_by_material; /* 1 = bin hits by material before shading     */
     int32_t blocks_per_sm;  /* persistent grid = SMs * this                  */
     int32_t use_graph;      /* 1 = replay iterations from a CUDA graph       */
-    int32_t iters_per_graph;/* iterations captured per graph                 */
-    int32_t reserved;
+    int32_t iters_per_graph;/* iterations between host checks of the queue  */
+    int32_t replicas;       /* sample replicas per pixel: 0 = automatic (small
+                               images get several slots per pixel, each with
+                               its own film copy), 1 = off, k = k copies     */
 } aqua_tuning;
 
 typedef struct aqua_stats {

@@ -69,11 +69,35 @@ def test_interior_textured_sample_matched(gpu_ctx):
 def test_launch_shape_does_not_change_the_image(gpu_ctx):
     s = gpu_ctx.procedural(2, seed=0, width=40, height=30)
     cfg = gpu_ctx.integrator(spp=32, max_depth=8, rr_depth=3, seed=9)
-    base, _ = gpu_ctx.render(s, cfg)
-    for kw in [dict(slots=1000), dict(slots=37), dict(sort_by_material=1), dict(block_trace=64, block_shade=32),
+    base, _ = gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning(replicas=1))
+    for kw in [dict(slots=1000), dict(slots=37), dict(sort_by_material=0), dict(block_trace=64, block_shade=32),
                dict(slots=333, sort_by_material=1, blocks_per_sm=2)]:
-        img, _ = gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning(**kw))
+        img, _ = gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning(replicas=1, **kw))
         assert np.array_equal(img.view(np.uint32), base.view(np.uint32)), kw
+    s.free()
+
+
+def test_sample_replicas(gpu_ctx):
+    """Small images run several slots per pixel, each on its own film copy:
+    deterministic for a given replica count, equal up to summation order
+    across counts, and the default for images below 2^20 pixels."""
+    import pyoracle
+
+    s = gpu_ctx.procedural(2, seed=0, width=40, height=30)
+    cfg = gpu_ctx.integrator(spp=32, max_depth=8, rr_depth=3, seed=9)
+    one, st1 = gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning(replicas=1))
+    four, st4 = gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning(replicas=4))
+    again, _ = gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning(replicas=4, sort_by_material=0, block_trace=64))
+    auto, sta = gpu_ctx.render(s, cfg)
+    assert np.array_equal(four, again)
+    np.testing.assert_allclose(four, one, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(auto, one, rtol=1e-5, atol=1e-6)
+    assert st1.paths == st4.paths == sta.paths == 40 * 30 * 32
+    # fewer iterations: the same work spread over more slots
+    assert sta.iterations < st1.iterations
+    o = pyoracle.OracleScene.from_aqua(s)
+    ref, _ = o.render(32, 8, seed=9, precision=64)
+    assert pyoracle.rel_mse(auto, ref) < TOL
     s.free()
 
 

@@ -56,7 +56,9 @@ def test_noalloc_matches_render_on_two_calls():
             noalloc_images.append((cfg, out.cpu().numpy().reshape(h, w, 3)))
         for (cfg, img), (w, h) in zip(noalloc_images, [(160, 120), (96, 64)]):
             scene.set_resolution(w, h)
-            ref, _ = ctx.render(scene, cfg)  # the existing entry point
+            # The existing entry point, with one path slot per pixel like the
+            # no-allocation variant (no sample replicas).
+            ref, _ = ctx.render(scene, cfg, tuning=ctx.tuning(replicas=1))
             assert np.isfinite(img).all()
             assert rel_mse(img, ref) < TOL
             assert np.array_equal(img, ref)
