@@ -171,7 +171,8 @@ NRC_PARAMS = 20672
 
 class NrcCfg(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
-                ("seed", C.c_uint64), ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3)]
+                ("seed", C.c_uint64), ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3),
+                ("ema_decay", C.c_float)]
 
 
 class Nrc:

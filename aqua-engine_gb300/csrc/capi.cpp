@@ -558,6 +558,8 @@ AQUA_API aqua_status aqua_nrc_create(aqua_ctx* ctx, const aqua_nrc_cfg* cfg, aqu
             n->net.beta1 = c.beta1;
             n->net.beta2 = c.beta2;
             n->net.eps = c.eps;
+            need(c.ema_decay >= 0.0f && c.ema_decay < 1.0f, "ema_decay must be in [0, 1)");
+            n->net.ema_decay = c.ema_decay;
             for (int i = 0; i < 3; ++i) {
                 n->net.bmin[i] = c.bbox_min[i];
                 n->net.bext[i] = c.bbox_max[i] - c.bbox_min[i];

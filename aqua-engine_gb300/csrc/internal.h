@@ -69,6 +69,9 @@ struct NrcNet {
     uint2* frag = nullptr;   // forward B fragments
     uint2* fragT = nullptr;  // backward B fragments
     double* loss = nullptr;  // loss sum of the last step
+    float* ema = nullptr;    // exponential moving average of w (inference weights)
+    uint2* frag_inf = nullptr;  // forward fragments of the inference weights
+    float ema_decay = 0.0f;  // 0 = inference uses w itself
     DevBuf train;            // training scratch, sized by train_rows
     int train_rows = 0;
     float* ty = nullptr;       // forward outputs (rows x 3)
@@ -93,6 +96,8 @@ struct NrcWorkspace {
     float* q_pred = nullptr;     // cache output per query
     float4* rec = nullptr;       // training-vertex records (6 words each)
     float4* ltrain = nullptr;    // radiance per training path
+    float4* lsnap = nullptr;     // per training path and bounce: radiance before it
+    size_t snaps = 0;            // bounces per training path (capacity)
     float* t_raw = nullptr;      // permuted training features
     uint16_t* t_x = nullptr;     // encoded training inputs
     float* t_target = nullptr;   // training targets

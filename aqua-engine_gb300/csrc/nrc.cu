@@ -72,7 +72,7 @@ __global__ void k_nrc_pack(const float* __restrict__ w, uint2* __restrict__ fwd,
         fwd[i] = make_uint2(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]));
     }
     int j = i - kFragFwd;
-    if (j >= 0 && j < kFragBwd) {
+    if (bwd && j >= 0 && j < kFragBwd) {
         int lane = j & 31, r = lane >> 2, c2 = (lane & 3) * 2;
         float v[4];
         if (j < 8 * 32) {
@@ -315,7 +315,8 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad(const uint32_t* __restrict__ 
 // partials in chunk order (deterministic).
 __global__ void k_nrc_adam(const float* __restrict__ partial, int chunks, float* __restrict__ w,
                            float* __restrict__ m, float* __restrict__ v, float* __restrict__ grad, float lr,
-                           float b1, float b2, float eps, float c1, float c2) {
+                           float b1, float b2, float eps, float c1, float c2, float* __restrict__ ema,
+                           float ema_decay) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= kNrcParams) return;
     float g = 0.0f;
@@ -325,7 +326,10 @@ __global__ void k_nrc_adam(const float* __restrict__ partial, int chunks, float*
     float vv = b2 * v[p] + (1.0f - b2) * g * g;
     m[p] = mm;
     v[p] = vv;
-    w[p] -= lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+    float wn = w[p] - lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+    w[p] = wn;
+    // Inference weights: exponential moving average of the trained ones.
+    if (ema_decay > 0.0f) ema[p] = ema_decay * ema[p] + (1.0f - ema_decay) * wn;
 }
 
 // ---------------------------------------------------------------- encoding
@@ -350,7 +354,8 @@ void nrc_alloc(aqua_ctx* ctx, NrcNet& net) {
     size_t off = 0;
     auto take = [&](size_t b) { size_t o = off; off = rup(off + b, 256); return o; };
     size_t o_w = take(4 * kNrcParams), o_m = take(4 * kNrcParams), o_v = take(4 * kNrcParams),
-           o_g = take(4 * kNrcParams), o_f = take(8 * kFragFwd), o_b = take(8 * kFragBwd), o_l = take(64);
+           o_g = take(4 * kNrcParams), o_f = take(8 * kFragFwd), o_b = take(8 * kFragBwd), o_l = take(64),
+           o_e = take(4 * kNrcParams), o_fi = take(8 * kFragFwd);
     dev_alloc(ctx, net.block, off);
     char* b = (char*)net.block.ptr;
     net.w = (float*)(b + o_w);
@@ -360,6 +365,8 @@ void nrc_alloc(aqua_ctx* ctx, NrcNet& net) {
     net.frag = (uint2*)(b + o_f);
     net.fragT = (uint2*)(b + o_b);
     net.loss = (double*)(b + o_l);
+    net.ema = (float*)(b + o_e);
+    net.frag_inf = (uint2*)(b + o_fi);
 }
 
 void nrc_release(NrcNet& net) {
@@ -384,6 +391,9 @@ void nrc_init_weights(aqua_ctx* ctx, NrcNet& net, uint64_t seed) {
 void nrc_pack(aqua_ctx* ctx, NrcNet& net) {
     int total = kFragFwd + kFragBwd;
     k_nrc_pack<<<(total + 255) / 256, 256, 0, ctx->stream>>>(net.w, net.frag, net.fragT);
+    // Forward fragments of the inference weights (the EMA when enabled).
+    k_nrc_pack<<<(kFragFwd + 255) / 256, 256, 0, ctx->stream>>>(net.ema_decay > 0.0f ? net.ema : net.w,
+                                                               net.frag_inf, nullptr);
     AQ_CUDA(cudaGetLastError());
 }
 
@@ -392,6 +402,7 @@ void nrc_set_weights(aqua_ctx* ctx, NrcNet& net, const float* host_w) {
     AQ_CUDA(cudaMemsetAsync(net.m, 0, 4 * kNrcParams, ctx->stream));
     AQ_CUDA(cudaMemsetAsync(net.v, 0, 4 * kNrcParams, ctx->stream));
     AQ_CUDA(cudaMemsetAsync(net.grad, 0, 4 * kNrcParams, ctx->stream));
+    AQ_CUDA(cudaMemcpyAsync(net.ema, net.w, 4 * kNrcParams, cudaMemcpyDeviceToDevice, ctx->stream));
     net.step = 0;
     nrc_pack(ctx, net);
     AQ_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -406,7 +417,7 @@ static int nrc_grid(aqua_ctx* ctx, int rows) {
 void nrc_forward_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, int n, float* out) {
     if (n <= 0) return;
     k_nrc_forward<false><<<nrc_grid(ctx, n), 128, 0, ctx->stream>>>(reinterpret_cast<const uint32_t*>(X), n,
-                                                                     net.frag, out, nullptr);
+                                                                     net.frag_inf, out, nullptr);
     AQ_CUDA(cudaGetLastError());
 }
 
@@ -444,7 +455,8 @@ void nrc_train_step_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, const flo
     net.step++;
     float c1 = 1.0f - powf(net.beta1, (float)net.step), c2 = 1.0f - powf(net.beta2, (float)net.step);
     k_nrc_adam<<<(kNrcParams + 255) / 256, 256, 0, st>>>(net.partial, chunks, net.w, net.m, net.v, net.grad, net.lr,
-                                                         net.beta1, net.beta2, net.eps, c1, c2);
+                                                         net.beta1, net.beta2, net.eps, c1, c2, net.ema,
+                                                         net.ema_decay);
     nrc_pack(ctx, net);
     AQ_CUDA(cudaGetLastError());
     net.launches += 5;

@@ -8,14 +8,19 @@
 // end paths early.
 //
 // Network: 64 inputs -> 5 hidden layers of 64 (ReLU) -> 3 outputs (RGB
-// radiance), no biases (input 62 is a constant 1). Weights are stored
+// radiance), no biases (input 63 is a constant 1). Weights are stored
 // row-major [out][in]: W1..W5 64x64, W6 3x64 = 20,672 parameters.
 //
-// Input encoding (64 values) of a path vertex: position (frequency encoding,
-// 6 octaves of sin/cos per axis over the scene box), outgoing direction and
-// normal (spherical coordinates, one-blob with 4 bins each; Mueller et al.
-// 2019, "Neural Importance Sampling"), roughness (one-blob, 4 bins), diffuse
-// and specular albedo, a constant 1 and a 0.
+// Input encoding (64 values) of a path vertex:
+//   0..47  position: frequency encoding, 8 octaves of sin/cos per axis over
+//          the scene box (finest period 1/128 of the box)
+//   48..53 outgoing direction: spherical coordinates, one-blob with 3 bins
+//          each (Mueller et al. 2019, "Neural Importance Sampling")
+//   54..57 normal: spherical coordinates, one-blob with 2 bins each
+//   58     roughness
+//   59..61 diffuse albedo
+//   62     luminance of the specular F0
+//   63     constant 1
 #pragma once
 
 #include <math.h>
@@ -57,27 +62,27 @@ AQ_HD void sph01(float x, float y, float z, float& u, float& v) {
 
 // Encoded value c (0..63) of a vertex; pn = position normalised to [0,1]^3.
 AQ_HD float nrc_encode_one(const NrcRaw& r, const float pn[3], int c) {
-    if (c < 36) {
-        int axis = c / 12, f = (c % 12) / 2;
+    if (c < 48) {
+        int axis = c / 16, f = (c % 16) / 2;
         float x = pn[axis] * (float)(1 << f) * kPi;
         return (c & 1) ? cosf(x) : sinf(x);
     }
-    if (c < 44) {
+    if (c < 54) {
         float u, v;
         sph01(r.w[0], r.w[1], r.w[2], u, v);
-        int k = c - 36;
-        return one_blob(k < 4 ? u : v, k & 3, 4);
+        int k = c - 48;
+        return one_blob(k < 3 ? u : v, k % 3, 3);
     }
-    if (c < 52) {
+    if (c < 58) {
         float u, v;
         sph01(r.n[0], r.n[1], r.n[2], u, v);
-        int k = c - 44;
-        return one_blob(k < 4 ? u : v, k & 3, 4);
+        int k = c - 54;
+        return one_blob(k < 2 ? u : v, k & 1, 2);
     }
-    if (c < 56) return one_blob(nrc_wrap01(r.rough), c - 52, 4);
-    if (c < 59) return r.kd[c - 56];
-    if (c < 62) return r.ks[c - 59];
-    return c == 62 ? 1.0f : 0.0f;
+    if (c == 58) return nrc_wrap01(r.rough);
+    if (c < 62) return r.kd[c - 59];
+    if (c == 62) return 0.2126f * r.ks[0] + 0.7152f * r.ks[1] + 0.0722f * r.ks[2];
+    return 1.0f;
 }
 
 }  // namespace aq

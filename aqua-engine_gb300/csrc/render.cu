@@ -36,6 +36,8 @@ struct WaveParams {
     uint32_t train_thresh;     // path trains when its 24-bit hash < this
     uint32_t max_train_paths;  // capacity of the per-training-path accumulators
     uint32_t max_records;      // capacity of the training-vertex records
+    int32_t train_span;        // reflections a target covers: max_depth - query_depth
+    int32_t train_depth;       // bounce limit of training paths: max_depth + train_span
     int32_t visualize;         // 1 = the image is the cache seen at the first hit
     // Sample replicas (0 or 1 = off). With K > 1 there are K slots per pixel:
     // slot s = r * pixels + p runs samples r, r + K, r + 2K, ... of pixel p
@@ -63,6 +65,8 @@ struct WavePtrs {
     float* q_raw;     // per query: 16 raw vertex features
     float4* rec;      // per training vertex: 6 words (raw 16, throughput 3, radiance-before 3, path id)
     float4* ltrain;   // per training path: radiance gathered so far
+    float4* lsnap;    // per training path and bounce k < train_depth: radiance
+                      // gathered before bounce k reflected anything (x < 0: unset)
 };
 
 // Counters of the cache mode (after the material buckets).
@@ -157,6 +161,8 @@ __device__ __forceinline__ bool start_path(const DevScene& S, const WaveParams& 
             uint32_t id = atomicAdd(&W.counters[kCntTrainPath], 1u);
             if (id < P.max_train_paths) {
                 W.ltrain[id] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                float4* snap = W.lsnap + (size_t)id * (size_t)P.train_depth;
+                for (int k = 0; k < P.train_depth; ++k) snap[k] = make_float4(-1.0f, 0.0f, 0.0f, 0.0f);
                 tag = (id + 1u) << 8;
             }
         }
@@ -360,7 +366,11 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtr
                     if (NRC && tag) ltrain_add(W.ltrain, train_id, thr * f3(L.le) * w);
                 }
             }
-            if ((int)depth < P.max_depth) {
+            // Training paths run train_span bounces past the last vertex
+            // they record, so every target covers the same reflections as
+            // the path the cache replaces.
+            const int depth_limit = (NRC && tag) ? P.train_depth : P.max_depth;
+            if ((int)depth < depth_limit) {
                 if (dot(ng, wo) < 0.0f) ng = -ng;
                 DevMaterial m = S.mats[info & 0xffffu];
                 v3 base = f3(m.a);
@@ -383,15 +393,16 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtr
                         nrc_raw(W.q_raw + 16 * (size_t)k, p, wo, ng, m.b.y, kd, B.F0);
                         queried = true;
                     } else if (tag) {
-                        uint32_t k = atomicAdd(&W.counters[kCntRecord], 1u);
+                        float4 lb = W.ltrain[train_id];
+                        W.lsnap[(size_t)train_id * (size_t)P.train_depth + depth] = lb;
+                        uint32_t k = (int)depth < P.max_depth ? atomicAdd(&W.counters[kCntRecord], 1u) : 0xffffffffu;
                         if (k < P.max_records) {
                             float r[24];
                             nrc_raw(r, p, wo, ng, m.b.y, kd, B.F0);
-                            float4 lb = W.ltrain[train_id];
                             r[16] = thr.x; r[17] = thr.y; r[18] = thr.z;
                             r[19] = lb.x; r[20] = lb.y; r[21] = lb.z;
                             r[22] = __int_as_float((int)train_id);
-                            r[23] = 0.0f;
+                            r[23] = __int_as_float((int)depth);
                             float4* dst = W.rec + 6 * (size_t)k;
 #pragma unroll
                             for (int q = 0; q < 6; ++q)
@@ -827,16 +838,26 @@ constexpr float kNrcMinThroughput = 1e-3f;
 constexpr float kNrcMaxTarget = 1e3f;
 
 __global__ void k_nrc_targets(const float4* __restrict__ rec, uint32_t n, const float4* __restrict__ ltrain,
-                              uint64_t a, uint64_t b, float* __restrict__ raw_out, float* __restrict__ t_out) {
+                              const float4* __restrict__ lsnap, int train_span, int train_depth, uint64_t a,
+                              uint64_t b, float* __restrict__ raw_out, float* __restrict__ t_out) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4* r = rec + 6 * (size_t)i;
         uint32_t j = (uint32_t)((a * (uint64_t)i + b) % (uint64_t)n);
         float4* ro = reinterpret_cast<float4*>(raw_out + 16 * (size_t)j);
         ro[0] = r[0]; ro[1] = r[1]; ro[2] = r[2]; ro[3] = r[3];
         float4 w4 = r[4], w5 = r[5];
-        // w4 = (beta.xyz, L_before.x), w5 = (L_before.yz, id, 0)
+        // w4 = (beta.xyz, L_before.x), w5 = (L_before.yz, id, depth d).
+        // Radiance of reflections d .. d + span - 1 = (gathered before bounce
+        // d + span) - (gathered before bounce d); past the path's end the
+        // path's total.
         uint32_t id = (uint32_t)__float_as_int(w5.z);
+        int d = __float_as_int(w5.w);
         float4 L = ltrain[id];
+        int k = d + train_span;
+        if (k < train_depth) {
+            float4 s = lsnap[(size_t)id * (size_t)train_depth + k];
+            if (s.x >= 0.0f) L = s;
+        }
         float t0 = fmaxf(L.x - w4.w, 0.0f) / fmaxf(w4.x, kNrcMinThroughput);
         float t1 = fmaxf(L.y - w5.x, 0.0f) / fmaxf(w4.y, kNrcMinThroughput);
         float t2 = fmaxf(L.z - w5.y, 0.0f) / fmaxf(w4.z, kNrcMinThroughput);
@@ -846,17 +867,19 @@ __global__ void k_nrc_targets(const float4* __restrict__ rec, uint32_t n, const 
     }
 }
 
-static void ensure_nrc_workspace(aqua_ctx* ctx, size_t queries, size_t records) {
+static void ensure_nrc_workspace(aqua_ctx* ctx, size_t queries, size_t records, size_t snaps) {
     NrcWorkspace& w = ctx->nrc_ws;
-    if (w.block.ptr && w.queries >= queries && w.records >= records) return;
+    if (w.block.ptr && w.queries >= queries && w.records >= records && w.snaps >= snaps) return;
     queries = std::max(queries, w.queries);
     records = std::max(records, w.records);
+    snaps = std::max(snaps, w.snaps);
     dev_free(w.block);
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
     size_t o_qp = take(16 * queries), o_qr = take(64 * queries), o_qx = take(128 * queries),
            o_qo = take(12 * queries), o_rec = take(96 * records), o_lt = take(16 * records),
-           o_tr = take(64 * records), o_tx = take(128 * records), o_tt = take(12 * records);
+           o_tr = take(64 * records), o_tx = take(128 * records), o_tt = take(12 * records),
+           o_sn = take(16 * records * snaps);
     dev_alloc(ctx, w.block, off);
     char* b = (char*)w.block.ptr;
     w.q_pix = (float4*)(b + o_qp);
@@ -868,8 +891,10 @@ static void ensure_nrc_workspace(aqua_ctx* ctx, size_t queries, size_t records) 
     w.t_raw = (float*)(b + o_tr);
     w.t_x = (uint16_t*)(b + o_tx);
     w.t_target = (float*)(b + o_tt);
+    w.lsnap = (float4*)(b + o_sn);
     w.queries = queries;
     w.records = records;
+    w.snaps = snaps;
 }
 
 static uint64_t gcd64(uint64_t a, uint64_t b) {
@@ -896,7 +921,10 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     ensure_workspace(ctx, slots, nb, pixels * plan.replicas);
     size_t cap_q = pixels * (size_t)cfg.spp;
     size_t cap_r = std::max<size_t>((size_t)cfg.nrc_train_samples, 1);
-    ensure_nrc_workspace(ctx, cap_q, cap_r);
+    const int query_depth = cfg.visualize_cache ? 0 : std::max(0, cfg.nrc_query_vertex - 1);
+    const int train_span = std::max(1, cfg.max_depth - query_depth);
+    const int train_depth = std::min(cfg.max_depth + train_span, 250);
+    ensure_nrc_workspace(ctx, cap_q, cap_r, (size_t)train_depth);
     Workspace& w = ctx->ws;
     NrcWorkspace& nw = ctx->nrc_ws;
     cudaStream_t st = ctx->stream;
@@ -922,7 +950,7 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     P.slots = (uint32_t)slots;
     P.pixels = (uint32_t)pixels;
     P.nb = (uint32_t)nb;
-    P.query_depth = visualize ? 0 : std::max(0, cfg.nrc_query_vertex - 1);
+    P.query_depth = query_depth;
     // Fraction of paths that train: aimed at nrc_train_samples records per
     // frame (first frame: assume 3 recorded vertices per training path).
     double frac = 0.0;
@@ -933,12 +961,14 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     P.train_thresh = (uint32_t)std::min(16777216.0, frac * 16777216.0);
     P.max_train_paths = (uint32_t)cap_r;
     P.max_records = (uint32_t)cap_r;
+    P.train_span = train_span;
+    P.train_depth = train_depth;
     P.visualize = visualize ? 1 : 0;
     WavePtrs W{};
     W.ray_o = w.ray_o; W.ray_d = w.ray_d; W.hit = w.hit; W.tp = w.tp; W.pst = w.pst;
     W.bucket = w.bucket; W.sh_o = w.sh_o; W.sh_d = w.sh_d; W.sh_c = w.sh_c; W.film = w.film;
     W.counters = w.counters; W.stats = w.stats;
-    W.q_pix = nw.q_pix; W.q_raw = nw.q_raw; W.rec = nw.rec; W.ltrain = nw.ltrain;
+    W.q_pix = nw.q_pix; W.q_raw = nw.q_raw; W.rec = nw.rec; W.ltrain = nw.ltrain; W.lsnap = nw.lsnap;
 
     auto trace_k = sorted ? k_trace_ext<true, false> : k_trace_ext<false, false>;
     auto shade_k = sorted ? k_shade<true, true> : k_shade<false, true>;
@@ -966,7 +996,7 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     }
     const int chunk = tune.iters_per_graph > 0 ? tune.iters_per_graph : 16;
     const uint64_t max_iters =
-        (uint64_t)(cfg.max_depth + 2) * (uint64_t)cfg.spp * ((pixels + slots - 1) / slots) + 64;
+        (uint64_t)(train_depth + 2) * (uint64_t)cfg.spp * ((pixels + slots - 1) / slots) + 64;
     uint64_t iter = 0;
     unsigned int* pc = ctx->pinned_counter;
     while (true) {
@@ -1006,7 +1036,8 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
         if (a == 0) a = 1;
         while (gcd64(a, nrec) != 1) ++a;
         int g = (int)std::min<size_t>((nrec + 255) / 256, (size_t)ctx->num_sms * 16);
-        k_nrc_targets<<<g, 256, 0, st>>>(nw.rec, nrec, nw.ltrain, a, b, nw.t_raw, nw.t_target);
+        k_nrc_targets<<<g, 256, 0, st>>>(nw.rec, nrec, nw.ltrain, nw.lsnap, train_span, train_depth, a, b, nw.t_raw,
+                                          nw.t_target);
         AQ_CUDA(cudaGetLastError());
         nrc_encode_dev(ctx, net, nw.t_raw, (int)nrec, nw.t_x);
         launches += 2;

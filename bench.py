@@ -162,6 +162,113 @@ def cpu_sample_run(threads: int, target_s: float, seed: int = 0):
                                   f"({int(paths)} paths, {dt:.1f} s)"
 
 
+NRC_WORKLOAD = {"workload": "interior-320x180-depth8-cache-vs-plain",
+                "scene": "synthetic interior: 153 meshes, 1.15M triangles, 8 textures 2048^2, 16 quad lights, seed 0",
+                "width": 320, "height": 180, "max_depth": 8, "rr_depth": 3, "reference_spp": 65536,
+                "frame_spp": 32, "train_records_per_frame": 65536, "batch": 16384, "learning_rate": 1e-2,
+                "query_vertex": 2, "burn_in_frames": 8, "target_relmse": 1e-3, "ema_decay": 0.0,
+                "note": "config 4 scaled to 320x180: 32 spp per frame keeps 1.8M paths and 65,536 training "
+                        "records per frame, as at 1080p and 1 spp"}
+
+
+_NRC_REF = {}
+
+
+def run_nrc_metric(ctx, budget_s: float = 60.0, overrides: dict | None = None):
+    """Time to relMSE 1e-3 against a 65,536-spp plain reference, for the plain
+    wavefront path tracer and for the cached renderer (online training
+    included in its time). Wall clock per render call; the error evaluation
+    between calls is excluded."""
+    import aqua
+    import numpy as np
+
+    W = dict(NRC_WORKLOAD, **(overrides or {}))
+    scene = ctx.procedural(3, seed=0, width=W["width"], height=W["height"])
+    shape = (W["height"], W["width"], 3)
+
+    def rel_mse(x, r):
+        return float(np.mean((x.astype(np.float64) - r) ** 2 / (r * r + 1e-2)))
+
+    # Reference: 65,536 spp as 16 progressive calls (kept for later calls
+    # with the same image size in this process).
+    t0 = time.perf_counter()
+    key = (W["width"], W["height"], W["reference_spp"], W["max_depth"])
+    if key not in _NRC_REF:
+        acc = np.zeros(shape, np.float32)
+        chunk = W["reference_spp"] // 16
+        for k in range(16):
+            ctx.render(scene, ctx.integrator(spp=chunk, max_depth=W["max_depth"], rr_depth=W["rr_depth"],
+                                             seed=424242, spp_offset=k * chunk), out=acc,
+                       flags=aqua.RENDER_ACCUMULATE)
+        _NRC_REF[key] = acc.astype(np.float64) / W["reference_spp"]
+    ref = _NRC_REF[key]
+    t_ref = time.perf_counter() - t0
+
+    # Plain: 16 spp per call, running mean.
+    plain = {"spp": 0, "t": 0.0, "curve": []}
+    acc = np.zeros(shape, np.float32)
+    t_plain, e = None, 1.0
+    while plain["t"] < budget_s:
+        t0 = time.perf_counter()
+        ctx.render(scene, ctx.integrator(spp=16, max_depth=W["max_depth"], rr_depth=W["rr_depth"], seed=7,
+                                         spp_offset=plain["spp"]), out=acc, flags=aqua.RENDER_ACCUMULATE)
+        plain["t"] += time.perf_counter() - t0
+        plain["spp"] += 16
+        e = rel_mse(acc / plain["spp"], ref)
+        if plain["spp"] % 256 == 0:
+            plain["curve"].append((plain["spp"], round(plain["t"], 4), e))
+        if e <= W["target_relmse"]:
+            t_plain = plain["t"]
+            break
+    plain["relmse"] = e
+
+    # Cached: frames of 32 spp with online training; frames after the
+    # burn-in are averaged.
+    net = aqua.Nrc(ctx, seed=1, learning_rate=W["learning_rate"], ema_decay=W["ema_decay"])
+    cfg = lambda f: ctx.integrator(type=aqua.INTEGRATOR_NRC, spp=W["frame_spp"], max_depth=W["max_depth"],
+                                   rr_depth=W["rr_depth"], seed=1000 + f, nrc_query_vertex=W["query_vertex"],
+                                   nrc_train_samples=W["train_records_per_frame"], batch_size=W["batch"],
+                                   training_iters=0)
+    cached = {"frames": 0, "t": 0.0, "curve": [], "nrc_ms": 0.0}
+    acc = np.zeros(shape, np.float32)
+    frame_img = np.zeros(shape, np.float32)
+    t_cached, e, used = None, 1.0, 0
+    best = 1.0
+    while cached["t"] < budget_s:
+        t0 = time.perf_counter()
+        _, st = ctx.render_nrc(scene, cfg(cached["frames"]), net, out=frame_img)
+        cached["t"] += time.perf_counter() - t0
+        cached["nrc_ms"] += st.nrc_ms
+        cached["frames"] += 1
+        if cached["frames"] > W["burn_in_frames"]:
+            acc += frame_img
+            used += 1
+            e = rel_mse(acc / used, ref)
+            best = min(best, e)
+            if t_plain and "relmse_at_plain_time" not in cached and cached["t"] >= t_plain:
+                cached["relmse_at_plain_time"] = e
+            if used % 16 == 0:
+                cached["curve"].append((cached["frames"], round(cached["t"], 4), e))
+            if e <= W["target_relmse"]:
+                t_cached = cached["t"]
+                break
+    cached["relmse"] = e
+    cached["best_relmse"] = best
+    net.free()
+    scene.free()
+    # The reference's own error, extrapolated from the plain curve (1/N).
+    ref_err = plain["relmse"] * plain["spp"] / W["reference_spp"]
+    out = {"config": W, "reference_s": round(t_ref, 2), "reference_relmse_est": ref_err,
+           "plain": {"time_s": t_plain, "spp": plain["spp"], "relmse": plain["relmse"], "curve": plain["curve"][-6:]},
+           "cached": {"time_s": t_cached, "frames": cached["frames"], "relmse": cached["relmse"],
+                      "best_relmse": best, "mlp_ms_total": round(cached["nrc_ms"], 2),
+                      "relmse_at_plain_time": cached.get("relmse_at_plain_time"),
+                      "curve": cached["curve"][-6:]},
+           "time_ratio_cached_over_plain": (t_cached / t_plain) if (t_cached and t_plain) else None,
+           "budget_s": budget_s}
+    return out
+
+
 def run_reference(args, world, rank, pg):
     if rank != 0:
         return
@@ -267,6 +374,10 @@ def run_gpu(args, world, rank, local, pg):
     e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
     e2e_value = sum_over_ranks(pg, e2e_paths) / e2e_s / 1e6
 
+    nrc = None
+    if rank == 0 and not args.no_nrc:
+        nrc = run_nrc_metric(ctx, args.nrc_budget)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -288,6 +399,7 @@ def run_gpu(args, world, rank, local, pg):
                 "e2e": {"value": e2e_value, "unit": "Mpaths/s", "h2d_bytes_per_step": int(info.upload_bytes),
                         "d2h_bytes_per_step": int(info.width * info.height * 12)},
                 "gpu_launches": gpu_launches,
+                "nrc_time_to_relmse": nrc,
                 "stage_ms_per_step": {"trace": trace_ms / args.steps,
                                       "shade": sum(s.shade_ms for s in steps) / args.steps,
                                       "shadow": sum(s.shadow_ms for s in steps) / args.steps}}
@@ -304,6 +416,8 @@ def main():
     ap.add_argument("--impl", default="aqua", choices=["aqua", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-nrc", action="store_true", help="skip the cached-vs-plain time-to-relMSE measurement")
+    ap.add_argument("--nrc-budget", type=float, default=60.0, help="seconds per arm of that measurement")
     ap.add_argument("--traffic-per-launch", type=float, default=None,
                     help="DRAM bytes per k_trace_ext launch from an ncu capture")
     ap.add_argument("--spp", type=int, default=0,

@@ -322,6 +322,9 @@ typedef struct aqua_nrc_cfg {
     float beta1, beta2, eps;      /* Adam moments                           */
     uint64_t seed;                /* He-uniform initial weights             */
     float bbox_min[3], bbox_max[3]; /* box that normalises positions        */
+    float ema_decay;              /* > 0: inference (aqua_nrc_forward and the
+                                     cached renderer) uses an exponential
+                                     moving average of the trained weights  */
 } aqua_nrc_cfg;
 
 AQUA_API void aqua_nrc_defaults(aqua_nrc_cfg* cfg);

@@ -681,8 +681,9 @@ void encode_row(const float* r, const float* bmin, const float* bmax, float* x) 
         u = std::min(std::max(u, 0.0), 1.0);
         v = std::min(std::max(v, 0.0), 1.0);
     };
-    auto blob = [](double v, int b) {
-        double d = (v - (b + 0.5) / 4.0) * 4.0;
+    // One-blob: Gaussian of width 1/k centred on bin b of k.
+    auto blob = [](double v, int b, int k) {
+        double d = (v - (b + 0.5) / k) * k;
         return std::exp(-0.5 * d * d);
     };
     double du, dv, nu, nv;
@@ -691,24 +692,24 @@ void encode_row(const float* r, const float* bmin, const float* bmax, float* x) 
     double rough = std::min(std::max((double)r[9], 0.0), 1.0);
     for (int c = 0; c < 64; ++c) {
         double v;
-        if (c < 36) {
-            int axis = c / 12, f = (c % 12) / 2;
+        if (c < 48) {  // position: 8 octaves of sin/cos per axis
+            int axis = c / 16, f = (c % 16) / 2;
             double a = pn[axis] * (double)(1 << f) * M_PI;
             v = (c & 1) ? std::cos(a) : std::sin(a);
-        } else if (c < 44) {
-            int k = c - 36;
-            v = blob(k < 4 ? du : dv, k & 3);
-        } else if (c < 52) {
-            int k = c - 44;
-            v = blob(k < 4 ? nu : nv, k & 3);
-        } else if (c < 56) {
-            v = blob(rough, c - 52);
-        } else if (c < 59) {
-            v = r[10 + (c - 56)];
+        } else if (c < 54) {  // direction: 3 bins per coordinate
+            int k = c - 48;
+            v = blob(k < 3 ? du : dv, k % 3, 3);
+        } else if (c < 58) {  // normal: 2 bins per coordinate
+            int k = c - 54;
+            v = blob(k < 2 ? nu : nv, k % 2, 2);
+        } else if (c == 58) {
+            v = rough;
         } else if (c < 62) {
-            v = r[13 + (c - 59)];
+            v = r[10 + (c - 59)];
+        } else if (c == 62) {
+            v = 0.2126 * r[13] + 0.7152 * r[14] + 0.0722 * r[15];
         } else {
-            v = c == 62 ? 1.0 : 0.0;
+            v = 1.0;
         }
         x[c] = (float)v;
     }

@@ -49,8 +49,11 @@ def test_encode_matches_oracle(net):
     x = net.encode(raw)
     ref = pyoracle.nrc_encode(raw, [-1, -1, -1], [1, 1, 1])
     got = pyoracle.bf16_to_float(x)
-    # bf16 keeps 8 significant bits; the device's sin/cos/exp add ~1e-6.
-    assert np.all(np.abs(got - ref) <= 2 ** -8 * np.abs(ref) + 1e-5)
+    # bf16 keeps 8 significant bits (half-ulp 2^-8 relative); the finest
+    # position octave (2^7 pi) turns the FP32 vs FP64 normalised position
+    # (~1e-7) into ~5e-5 absolute near sine zero crossings.
+    assert np.all(np.abs(got - ref) <= 2 ** -8 * np.abs(ref) + 2e-4)
+    assert np.abs(got - ref).mean() < 2e-3
 
 
 def test_forward_matches_oracle(net):

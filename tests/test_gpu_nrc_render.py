@@ -18,9 +18,9 @@ TOL = 1e-3
 
 
 def constant_weights(rgb):
-    """Weights whose output is `rgb` for every input (input 62 is 1)."""
+    """Weights whose output is `rgb` for every input (input 63 is 1)."""
     w = np.zeros(20672, np.float32)
-    w[0 * 4096 + 0 * 64 + 62] = 1.0
+    w[0 * 4096 + 0 * 64 + 63] = 1.0
     for l in range(1, 5):
         w[l * 4096 + 0] = 1.0
     for c in range(3):

@@ -128,9 +128,12 @@ def test_encoding_shape_and_ranges():
     raw[:, 10:16] = rng.uniform(0, 1, (500, 6))
     x = pyoracle.nrc_encode(raw, [-2, -2, -2], [2, 2, 2])
     assert x.shape == (500, 64)
-    assert np.all(np.abs(x[:, :36]) <= 1.0)
-    assert np.all((x[:, 36:56] > 0) & (x[:, 36:56] <= 1.0))
-    np.testing.assert_array_equal(x[:, 56:62], raw[:, 10:16])
-    assert np.all(x[:, 62] == 1.0) and np.all(x[:, 63] == 0.0)
+    assert np.all(np.abs(x[:, :48]) <= 1.0)
+    assert np.all((x[:, 48:58] > 0) & (x[:, 48:58] <= 1.0))  # one-blob bins
+    np.testing.assert_allclose(x[:, 58], raw[:, 9], rtol=1e-7)
+    np.testing.assert_array_equal(x[:, 59:62], raw[:, 10:13])
+    lum = 0.2126 * raw[:, 13] + 0.7152 * raw[:, 14] + 0.0722 * raw[:, 15]
+    np.testing.assert_allclose(x[:, 62], lum, rtol=1e-6)
+    assert np.all(x[:, 63] == 1.0)
     # sin^2 + cos^2 = 1 for every position octave
-    np.testing.assert_allclose(x[:, 0:36:2] ** 2 + x[:, 1:36:2] ** 2, 1.0, atol=1e-6)
+    np.testing.assert_allclose(x[:, 0:48:2] ** 2 + x[:, 1:48:2] ** 2, 1.0, atol=1e-6)
