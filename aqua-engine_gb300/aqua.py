@@ -150,6 +150,7 @@ SIGNATURES = [
                               C.POINTER(Stats)]),
     ("aqua_autotune", C.c_int, [_P, _P, C.POINTER(IntegratorCfg), C.POINTER(Tuning)]),
     ("aqua_render_batch", C.c_int, [_P, _P, C.c_size_t, C.POINTER(Tuning), C.POINTER(BatchStats)]),
+    ("aqua_autotune_batch", C.c_int, [_P, _P, C.c_size_t, C.POINTER(Tuning)]),
     ("aqua_workspace_bytes", C.c_uint64, [_P]),
     ("aqua_render_noalloc", C.c_int, [_P, _P, C.POINTER(IntegratorCfg), _P, C.POINTER(Stats)]),
     ("aqua_render_noalloc_max_pixels", C.c_uint64, []),
@@ -425,6 +426,31 @@ class Context:
                                          C.byref(tuning) if tuning is not None else None, C.c_void_p(dev_ptr),
                                          flags | RENDER_DEVICE_FILM, C.byref(st)))
         return st
+
+    def autotune(self, scene: Scene, cfg: IntegratorCfg) -> Tuning:
+        t = Tuning()
+        self._check(self.lib.aqua_autotune(self.handle, scene.handle, C.byref(cfg), C.byref(t)))
+        return t
+
+    def render_batch(self, jobs, tuning: Tuning | None = None):
+        """jobs: list of (scene, width, height, spp, max_depth, seed, device_ptr).
+        Returns (BatchStats, per-job completion ms)."""
+        arr = (Job * len(jobs))()
+        for i, (sc, w, h, spp, depth, seed, ptr) in enumerate(jobs):
+            arr[i] = Job(sc.handle, w, h, spp, depth, seed, ptr)
+        job_ms = (C.c_double * max(len(jobs), 1))()
+        st = BatchStats(0.0, 0, job_ms)
+        self._check(self.lib.aqua_render_batch(self.handle, arr, len(jobs),
+                                               C.byref(tuning) if tuning is not None else None, C.byref(st)))
+        return st, np.array(job_ms[:len(jobs)])
+
+    def autotune_batch(self, jobs) -> Tuning:
+        arr = (Job * len(jobs))()
+        for i, (sc, w, h, spp, depth, seed, ptr) in enumerate(jobs):
+            arr[i] = Job(sc.handle, w, h, spp, depth, seed, ptr)
+        t = Tuning()
+        self._check(self.lib.aqua_autotune_batch(self.handle, arr, len(jobs), C.byref(t)))
+        return t
 
     def workspace_bytes(self) -> int:
         return int(self.lib.aqua_workspace_bytes(self.handle))

@@ -1,0 +1,362 @@
+// batch.cu — batched rendering of many independent jobs (views of several
+// scenes, uneven resolutions and sample counts) in one persistent launch,
+// replayed from a captured CUDA graph.
+//
+// Work units are (job, 32 consecutive pixels). Each warp takes units from a
+// global atomic counter in job order; a lane owns one pixel of the unit and
+// runs all of that pixel's samples, summing contributions in the same order
+// as the wavefront (emission, then next-event estimation, bounce after
+// bounce), so a job's image matches aqua_render's. The last warp to finish a
+// job stamps the device clock, giving per-job completion latencies.
+//
+// Path semantics are those of the wavefront (render.cu): `Perspective`
+// camera (scenes/cbox.json:516-543), Lambert + GGX `Principled`
+// (scenes/cbox.json:3-62), point and area lights with power-heuristic MIS,
+// Russian roulette from bounce rr_depth, `max_depth` (integrator.json:5).
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "internal.h"
+#include "shading.cuh"
+
+namespace aq {
+
+constexpr int kUnitPixels = 32;
+
+__device__ __forceinline__ unsigned long long device_clock_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// One full path: camera ray, closest hits, emission with MIS, next-event
+// estimation with an any-hit shadow ray, BSDF sampling and Russian roulette.
+// Contributions are added to `sum` in the wavefront's order.
+__device__ __forceinline__ void trace_path(const DevScene& S, const DevCamera& cam, uint64_t seed, uint32_t pixel,
+                                           uint32_t sample, int max_depth, int rr_depth, const float* lut, v3& sum,
+                                           uint32_t& n_ext, uint32_t& n_shadow) {
+    uint32_t dummy0 = 0, dummy1 = 0;
+    uint64_t st = path_rng_state(seed, pixel, sample), inc = pixel_inc(pixel);
+    float u0 = draw(st, inc), u1 = draw(st, inc), u2 = draw(st, inc), u3 = draw(st, inc);
+    v3 o, dir;
+    camera_ray(cam, pixel, u0, u1, u2, u3, o, dir);
+    v3 thr = mk(1.0f, 1.0f, 1.0f);
+    float pdf_b = 0.0f;
+    for (int depth = 0;; ++depth) {
+        ++n_ext;
+        TraceResult h = traverse<false, false>(S, o, dir, 0.0f, INFINITY, dummy0, dummy1);
+        if (h.tri < 0) {
+            v3 e = mk(S.env[0], S.env[1], S.env[2]);
+            if (e.x > 0.0f || e.y > 0.0f || e.z > 0.0f) sum = sum + thr * e;
+            return;
+        }
+        const float4* tw = S.tris + 3 * (size_t)h.tri;
+        float4 a = ldg_(tw), b = ldg_(tw + 1), c = ldg_(tw + 2);
+        uint32_t info = (uint32_t)__float_as_int(b.w);
+        v3 v0 = f3(a), e1 = f3(b) - v0, e2 = f3(c) - v0;
+        v3 p = v0 + e1 * h.u + e2 * h.v;
+        v3 ng = normalize(cross(e1, e2));
+        v3 wo = -dir;
+        int light = (int)(info >> 16) - 1;
+        if (light >= 0) {
+            DevLight L = S.lights[light];
+            v3 nl = normalize(cross(f3(L.e1), f3(L.e2)));
+            float cos_l = dot(nl, wo);
+            if (cos_l > 0.0f) {
+                float w = 1.0f;
+                if (depth > 0 && pdf_b > 0.0f) {
+                    float pl = L.e2.w * h.t * h.t / (L.e1.w * cos_l);
+                    w = power_heuristic(pdf_b, pl);
+                }
+                sum = sum + thr * f3(L.le) * w;
+            }
+        }
+        if (depth >= max_depth) return;
+        if (dot(ng, wo) < 0.0f) ng = -ng;
+        DevMaterial m = S.mats[info & 0xffffu];
+        v3 base = f3(m.a);
+        int ti = __float_as_int(m.a.w);
+        if (ti >= 0) {
+            const float2* uv = S.uvs + 3 * (size_t)h.tri;
+            float2 t0 = ldg_(uv), t1 = ldg_(uv + 1), t2 = ldg_(uv + 2);
+            float w0 = 1.0f - h.u - h.v;
+            float tu = t0.x * w0 + t1.x * h.u + t2.x * h.v;
+            float tv = t0.y * w0 + t1.y * h.u + t2.y * h.v;
+            base = base * tex_bilinear(S, ti, tu, tv, lut);
+        }
+        Bsdf B = make_bsdf(base, m.b.x, m.b.y, m.b.z);
+        v3 T, Bt;
+        onb(ng, T, Bt);
+        v3 wol = mk(dot(wo, T), dot(wo, Bt), dot(wo, ng));
+        float u[kBounceDims];
+#pragma unroll
+        for (int k = 0; k < kBounceDims; ++k) u[k] = draw(st, inc);
+        if (S.n_lights > 0 && wol.z > 0.0f) {
+            DevLight L = S.lights[pick_light(S, u[0])];
+            int ty = __float_as_int(L.p0.w);
+            float pmf = L.e2.w;
+            v3 contrib = mk(0, 0, 0), wi;
+            float dist = 0.0f;
+            if (ty == AQUA_LIGHT_POINT) {
+                v3 dl = f3(L.p0) - p;
+                float d2 = dot(dl, dl);
+                dist = sqrtf(d2);
+                wi = dl * (1.0f / dist);
+                float cs = dot(wi, ng);
+                if (cs > 0.0f && d2 > 0.0f) {
+                    v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
+                    contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs / (d2 * pmf));
+                }
+            } else {
+                v3 le1 = f3(L.e1), le2 = f3(L.e2), xl;
+                if (ty == AQUA_LIGHT_QUAD) {
+                    xl = f3(L.p0) + le1 * u[1] + le2 * u[2];
+                } else {
+                    float su = sqrtf(u[1]);
+                    xl = f3(L.p0) + le1 * (su * (1.0f - u[2])) + le2 * (su * u[2]);
+                }
+                v3 nl = normalize(cross(le1, le2));
+                v3 dl = xl - p;
+                float d2 = dot(dl, dl);
+                dist = sqrtf(d2);
+                wi = dl * (1.0f / dist);
+                float cl = -dot(wi, nl), cs = dot(wi, ng);
+                if (cl > 0.0f && cs > 0.0f && d2 > 0.0f) {
+                    v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
+                    float pl = pmf * d2 / (L.e1.w * cl);
+                    float pb = bsdf_pdf(B, wol, wil);
+                    float w = power_heuristic(pl, pb);
+                    contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs * w / pl);
+                }
+            }
+            if (contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f) {
+                ++n_shadow;
+                v3 so = offset_ray(p, ng);
+                TraceResult sh = traverse<true, false>(S, so, wi, 0.0f, dist * (1.0f - 1e-4f), dummy0, dummy1);
+                if (sh.tri < 0) sum = sum + contrib;
+            }
+        }
+        v3 wil = bsdf_sample(B, wol, u[3], u[4], u[5]);
+        if (!(wil.z > 0.0f && wol.z > 0.0f)) return;
+        float pdf = bsdf_pdf(B, wol, wil);
+        v3 f = bsdf_eval(B, wol, wil);
+        if (!(pdf > 0.0f)) return;
+        thr = thr * f * (wil.z / pdf);
+        bool ok = maxc(thr) > 0.0f && isfinite(thr.x) && isfinite(thr.y) && isfinite(thr.z);
+        if (ok && depth >= rr_depth) {
+            float q = fminf(1.0f, maxc(thr));
+            if (u[6] >= q) ok = false;
+            else thr = thr * (1.0f / q);
+        }
+        if (!ok) return;
+        dir = normalize(T * wil.x + Bt * wil.y + ng * wil.z);
+        o = offset_ray(p, ng);
+        pdf_b = pdf;
+    }
+}
+
+// Persistent kernel over all jobs' work units. counters[0] = next unit,
+// counters[1 + j] = finished units of job j. clocks[0] = launch time,
+// clocks[1 + j] = completion time of job j.
+__global__ void k_batch(const DevScene* __restrict__ scenes, const DevJob* __restrict__ jobs, int njobs,
+                        uint32_t total_units, uint32_t* __restrict__ counters,
+                        unsigned long long* __restrict__ clocks, unsigned long long* __restrict__ stats) {
+    __shared__ float lut[256];
+    __shared__ uint32_t first_unit[kMaxBatchJobs + 1];
+    fill_srgb_lut(lut);
+    for (int j = threadIdx.x; j < njobs; j += blockDim.x) first_unit[j] = jobs[j].unit_begin;
+    if (threadIdx.x == 0) first_unit[njobs] = total_units;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&clocks[0], 0ull, device_clock_ns());
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    uint32_t n_ext = 0, n_sh = 0, n_paths = 0;
+    while (true) {
+        uint32_t unit = 0;
+        if (lane == 0) unit = atomicAdd(&counters[0], 1u);
+        unit = __shfl_sync(0xffffffffu, unit, 0);
+        if (unit >= total_units) break;
+        int lo = 0, hi = njobs - 1;
+        while (lo < hi) {  // last job whose first unit <= unit
+            int mid = (lo + hi + 1) >> 1;
+            if (first_unit[mid] <= unit) lo = mid;
+            else hi = mid - 1;
+        }
+        const DevJob& J = jobs[lo];
+        const DevScene& S = scenes[J.scene];
+        uint32_t pixel = (unit - J.unit_begin) * kUnitPixels + (uint32_t)lane;
+        if (pixel < J.pixels) {
+            v3 sum = mk(0.0f, 0.0f, 0.0f);
+            for (int s = 0; s < J.spp; ++s)
+                trace_path(S, J.cam, J.seed, pixel, (uint32_t)s, J.max_depth, J.rr_depth, lut, sum, n_ext, n_sh);
+            n_paths += (uint32_t)J.spp;
+            float inv = 1.0f / (float)J.spp;
+            J.out[3 * (size_t)pixel + 0] = sum.x * inv;
+            J.out[3 * (size_t)pixel + 1] = sum.y * inv;
+            J.out[3 * (size_t)pixel + 2] = sum.z * inv;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence();
+            uint32_t done = atomicAdd(&counters[1 + lo], 1u) + 1u;
+            if (done == J.units) clocks[1 + lo] = device_clock_ns();
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        n_ext += __shfl_down_sync(0xffffffffu, n_ext, o);
+        n_sh += __shfl_down_sync(0xffffffffu, n_sh, o);
+        n_paths += __shfl_down_sync(0xffffffffu, n_paths, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&stats[0], (unsigned long long)n_paths);
+        atomicAdd(&stats[1], (unsigned long long)n_ext);
+        atomicAdd(&stats[2], (unsigned long long)n_sh);
+    }
+}
+
+// ---------------------------------------------------------------- host side
+static bool same_batch(const BatchGraph& g, const std::vector<DevJob>& jobs, const std::vector<DevScene>& scenes,
+                       int block, int grid) {
+    return g.exec && g.block == block && g.grid == grid && g.jobs.size() == jobs.size() &&
+           g.scenes.size() == scenes.size() &&
+           memcmp(g.jobs.data(), jobs.data(), jobs.size() * sizeof(DevJob)) == 0 &&
+           memcmp(g.scenes.data(), scenes.data(), scenes.size() * sizeof(DevScene)) == 0;
+}
+
+void batch_release(aqua_ctx* ctx) {
+    BatchGraph& g = ctx->batch;
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+    dev_free(g.buf);
+    g = BatchGraph{};
+}
+
+void render_batch(aqua_ctx* ctx, const aqua_job* in, size_t n, const aqua_tuning& tune, aqua_batch_stats* stats) {
+    if (n == 0) return;
+    if (n > (size_t)kMaxBatchJobs) throw Error(AQUA_ERR_INVALID_ARG, "at most 1024 jobs per batch");
+    std::vector<DevScene> scenes;
+    std::map<const aqua_scene*, int> scene_index;
+    std::vector<DevJob> jobs(n);
+    uint32_t units = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const aqua_job& j = in[i];
+        if (!j.scene || !j.rgb_out) throw Error(AQUA_ERR_INVALID_ARG, "job " + std::to_string(i) + ": scene and rgb_out must be non-NULL");
+        if (j.width <= 0 || j.height <= 0 || j.width > 16384 || j.height > 16384)
+            throw Error(AQUA_ERR_INVALID_ARG, "job " + std::to_string(i) + ": resolution out of range");
+        if (j.spp <= 0 || j.max_depth < 0 || j.max_depth > 250)
+            throw Error(AQUA_ERR_INVALID_ARG, "job " + std::to_string(i) + ": spp must be > 0 and max_depth in [0, 250]");
+        if (((uintptr_t)j.rgb_out & 3) != 0) throw Error(AQUA_ERR_INVALID_ARG, "rgb_out must be 4-byte aligned");
+        auto it = scene_index.find(j.scene);
+        int si;
+        if (it == scene_index.end()) {
+            si = (int)scenes.size();
+            scene_index[j.scene] = si;
+            scenes.push_back(j.scene->ds);
+        } else {
+            si = it->second;
+        }
+        aqua_camera cam = j.scene->host.cam;
+        cam.width = j.width;
+        cam.height = j.height;
+        DevJob& d = jobs[i];
+        memset(&d, 0, sizeof(d));
+        d.cam = dev_camera(cam);
+        d.out = j.rgb_out;
+        d.seed = j.seed;
+        d.scene = si;
+        d.spp = j.spp;
+        d.max_depth = j.max_depth;
+        d.rr_depth = 3;
+        d.pixels = (uint32_t)j.width * (uint32_t)j.height;
+        d.units = (d.pixels + kUnitPixels - 1) / kUnitPixels;
+        d.unit_begin = units;
+        if ((uint64_t)units + d.units > 0xFFFFFFF0ull) throw Error(AQUA_ERR_INVALID_ARG, "too many pixels in the batch");
+        units += d.units;
+    }
+    int block = tune.block_trace > 0 ? tune.block_trace : 128;
+    if (block != 64 && block != 128 && block != 256) throw Error(AQUA_ERR_INVALID_ARG, "block size must be 64, 128 or 256");
+    int per_sm = tune.blocks_per_sm;
+    if (per_sm <= 0) {
+        AQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, block, 0));
+        per_sm = std::max(per_sm, 1);
+    }
+    int grid = ctx->num_sms * per_sm;
+    cudaStream_t st = ctx->stream;
+    BatchGraph& g = ctx->batch;
+    bool reuse = same_batch(g, jobs, scenes, block, grid) && tune.use_graph != 0;
+    if (!reuse) {
+        batch_release(ctx);
+        size_t off = 0;
+        auto take = [&](size_t b) { size_t o = off; off = (off + b + 255) / 256 * 256; return o; };
+        size_t o_s = take(sizeof(DevScene) * scenes.size()), o_j = take(sizeof(DevJob) * n),
+               o_c = take(4 * (n + 1)), o_t = take(8 * (n + 1)), o_st = take(8 * 4);
+        dev_alloc(ctx, g.buf, off);
+        char* b = (char*)g.buf.ptr;
+        g.d_scenes = (DevScene*)(b + o_s);
+        g.d_jobs = (DevJob*)(b + o_j);
+        g.d_counters = (uint32_t*)(b + o_c);
+        g.d_clocks = (unsigned long long*)(b + o_t);
+        g.d_stats = (unsigned long long*)(b + o_st);
+        AQ_CUDA(cudaMemcpyAsync(g.d_scenes, scenes.data(), sizeof(DevScene) * scenes.size(), cudaMemcpyHostToDevice, st));
+        AQ_CUDA(cudaMemcpyAsync(g.d_jobs, jobs.data(), sizeof(DevJob) * n, cudaMemcpyHostToDevice, st));
+        g.jobs = jobs;
+        g.scenes = scenes;
+        g.block = block;
+        g.grid = grid;
+        g.units = units;
+        // One launch of the whole batch: counter resets + the persistent kernel.
+        auto enqueue = [&](cudaStream_t s) {
+            AQ_CUDA(cudaMemsetAsync(g.d_counters, 0, 4 * (n + 1), s));
+            AQ_CUDA(cudaMemsetAsync(g.d_clocks, 0, 8 * (n + 1), s));
+            AQ_CUDA(cudaMemsetAsync(g.d_stats, 0, 8 * 4, s));
+            k_batch<<<grid, block, 0, s>>>(g.d_scenes, g.d_jobs, (int)n, units, g.d_counters, g.d_clocks, g.d_stats);
+            AQ_CUDA(cudaGetLastError());
+        };
+        if (tune.use_graph != 0) {
+            AQ_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            try {
+                enqueue(st);
+            } catch (...) {
+                cudaGraph_t tmp;
+                cudaStreamEndCapture(st, &tmp);
+                if (tmp) cudaGraphDestroy(tmp);
+                throw;
+            }
+            AQ_CUDA(cudaStreamEndCapture(st, &g.graph));
+            AQ_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
+        }
+    }
+    cudaEvent_t e0, e1;
+    AQ_CUDA(cudaEventCreate(&e0));
+    AQ_CUDA(cudaEventCreate(&e1));
+    AQ_CUDA(cudaEventRecord(e0, st));
+    if (g.exec) {
+        AQ_CUDA(cudaGraphLaunch(g.exec, st));
+    } else {
+        AQ_CUDA(cudaMemsetAsync(g.d_counters, 0, 4 * (n + 1), st));
+        AQ_CUDA(cudaMemsetAsync(g.d_clocks, 0, 8 * (n + 1), st));
+        AQ_CUDA(cudaMemsetAsync(g.d_stats, 0, 8 * 4, st));
+        k_batch<<<grid, block, 0, st>>>(g.d_scenes, g.d_jobs, (int)n, units, g.d_counters, g.d_clocks, g.d_stats);
+        AQ_CUDA(cudaGetLastError());
+    }
+    AQ_CUDA(cudaEventRecord(e1, st));
+    std::vector<unsigned long long> clocks(n + 1);
+    unsigned long long hs[4] = {0, 0, 0, 0};
+    AQ_CUDA(cudaMemcpyAsync(clocks.data(), g.d_clocks, 8 * (n + 1), cudaMemcpyDeviceToHost, st));
+    AQ_CUDA(cudaMemcpyAsync(hs, g.d_stats, 8 * 4, cudaMemcpyDeviceToHost, st));
+    AQ_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.0f;
+    AQ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (stats) {
+        stats->device_ms = ms;
+        stats->paths = hs[0];
+        if (stats->job_ms)
+            for (size_t i = 0; i < n; ++i)
+                stats->job_ms[i] = clocks[1 + i] >= clocks[0] ? (double)(clocks[1 + i] - clocks[0]) * 1e-6 : -1.0;
+    }
+}
+
+}  // namespace aq

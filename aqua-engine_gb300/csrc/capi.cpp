@@ -280,6 +280,7 @@ AQUA_API void aqua_destroy(aqua_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     workspace_release(ctx);
+    batch_release(ctx);
     dev_free(ctx->nrc_ws.block);
     dev_free(ctx->trace_rays);
     dev_free(ctx->trace_hits);
@@ -488,10 +489,84 @@ AQUA_API aqua_status aqua_render(aqua_ctx* ctx, aqua_scene* s, const aqua_integr
     });
 }
 
+// Autotuner: times short renders (at most 16 spp) of every candidate launch
+// shape, two runs each, and keeps the fastest by device time.
 AQUA_API aqua_status aqua_autotune(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg* cfg, aqua_tuning* out) {
     return guard(ctx, [&]() {
         need(s && cfg && out, "scene, cfg and out must be non-NULL");
-        throw Error(AQUA_ERR_UNSUPPORTED, "autotuner not built yet");
+        need_device(ctx);
+        if (cfg->type != AQUA_INTEGRATOR_PATH)
+            throw Error(AQUA_ERR_UNSUPPORTED, "the autotuner tunes the path integrator");
+        aqua_integrator_cfg c = *cfg;
+        c.spp = std::max(1, std::min(cfg->spp, 16));
+        size_t pixels = (size_t)s->host.cam.width * (size_t)s->host.cam.height;
+        DevBuf film;
+        dev_alloc(ctx, film, 12 * pixels);
+        aqua_tuning best;
+        aqua_tuning_defaults(&best);
+        double best_ms = 1e300;
+        try {
+            for (int sort : {0, 1})
+                for (int bt : {64, 128})
+                    for (int bs : {64, 128})
+                        for (int bps : {0, 4, 8}) {
+                            aqua_tuning t;
+                            aqua_tuning_defaults(&t);
+                            t.sort_by_material = sort;
+                            t.block_trace = bt;
+                            t.block_shade = bs;
+                            t.blocks_per_sm = bps;
+                            double ms = 0.0;
+                            for (int rep = 0; rep < 2; ++rep) {
+                                aqua_stats st;
+                                render_path(ctx, s, c, t, (float*)film.ptr, AQUA_RENDER_DEVICE_FILM, &st);
+                                if (rep == 1) ms = st.device_ms;
+                            }
+                            if (ms < best_ms) {
+                                best_ms = ms;
+                                best = t;
+                            }
+                        }
+        } catch (...) {
+            dev_free(film);
+            throw;
+        }
+        dev_free(film);
+        *out = best;
+    });
+}
+
+// Batch autotuner: block size x blocks per SM, timed on the same jobs with
+// their sample counts divided by 32 (at least 1).
+AQUA_API aqua_status aqua_autotune_batch(aqua_ctx* ctx, const aqua_job* jobs, size_t n, aqua_tuning* out) {
+    return guard(ctx, [&]() {
+        need(jobs && n > 0 && out, "jobs and out must be non-NULL and n > 0");
+        need_device(ctx);
+        std::vector<aqua_job> small(jobs, jobs + n);
+        for (auto& j : small) j.spp = std::max(1, j.spp / 32);
+        aqua_tuning best;
+        aqua_tuning_defaults(&best);
+        best.use_graph = 1;
+        double best_ms = 1e300;
+        for (int block : {64, 128, 256})
+            for (int bps : {0, 2, 4, 8}) {
+                aqua_tuning t;
+                aqua_tuning_defaults(&t);
+                t.block_trace = block;
+                t.blocks_per_sm = bps;
+                t.use_graph = 1;
+                double ms = 0.0;
+                for (int rep = 0; rep < 2; ++rep) {
+                    aqua_batch_stats st{};
+                    render_batch(ctx, small.data(), n, t, &st);
+                    if (rep == 1) ms = st.device_ms;
+                }
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = t;
+                }
+            }
+        *out = best;
     });
 }
 
@@ -499,9 +574,14 @@ AQUA_API aqua_status aqua_render_batch(aqua_ctx* ctx, const aqua_job* jobs, size
                                        aqua_batch_stats* stats) {
     return guard(ctx, [&]() {
         need(jobs != nullptr || n == 0, "jobs is NULL");
-        (void)tuning;
-        (void)stats;
-        throw Error(AQUA_ERR_UNSUPPORTED, "batched rendering not built yet");
+        need_device(ctx);
+        aqua_tuning t;
+        if (tuning) t = *tuning;
+        else {
+            aqua_tuning_defaults(&t);
+            t.use_graph = 1;
+        }
+        render_batch(ctx, jobs, n, t, stats);
     });
 }
 

@@ -103,6 +103,32 @@ struct NrcWorkspace {
     float* t_target = nullptr;   // training targets
 };
 
+// Batched rendering (batch.cu): one job as the persistent kernel sees it.
+constexpr int kMaxBatchJobs = 1024;
+struct DevJob {
+    DevCamera cam;           // the scene's camera at the job's resolution
+    float* out;              // width * height * 3 floats
+    uint64_t seed;
+    int32_t scene, spp, max_depth, rr_depth;
+    uint32_t pixels, unit_begin, units, pad;
+};
+
+// The last batch, kept so an identical batch replays its CUDA graph.
+struct BatchGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    DevBuf buf;
+    DevScene* d_scenes = nullptr;
+    DevJob* d_jobs = nullptr;
+    uint32_t* d_counters = nullptr;
+    unsigned long long* d_clocks = nullptr;
+    unsigned long long* d_stats = nullptr;
+    std::vector<DevJob> jobs;
+    std::vector<DevScene> scenes;
+    int block = 0, grid = 0;
+    uint32_t units = 0;
+};
+
 enum { kCntQ0 = 0, kCntQ1 = 1, kCntShadow = 2, kCntBucket0 = 8 };
 enum { kStatExt = 0, kStatShadow, kStatPaths, kStatNodes, kStatTris, kStatShNodes, kStatShTris, kStatCount };
 
@@ -135,6 +161,7 @@ struct aqua_ctx {
     uint64_t fail_alloc_after = 0;
     aq::Workspace ws;
     aq::NrcWorkspace nrc_ws;
+    aq::BatchGraph batch;
     unsigned int* pinned_counter = nullptr;  // host-mapped copy of queue counts
     std::vector<cudaEvent_t> events;         // pool for stage timing
     aq::DevBuf trace_rays, trace_hits;       // staging for host-pointer traces
@@ -163,6 +190,10 @@ void workspace_release(aqua_ctx* ctx);
 // queries and training paths, inference, online training.
 void render_nrc(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg& cfg, const aqua_tuning& tune,
                 aqua_nrc* nrc, float* rgb_out, uint32_t flags, aqua_stats* stats);
+
+// Batched rendering (batch.cu).
+void render_batch(aqua_ctx* ctx, const aqua_job* jobs, size_t n, const aqua_tuning& tune, aqua_batch_stats* stats);
+void batch_release(aqua_ctx* ctx);
 
 // Radiance-cache network (nrc.cu).
 void nrc_alloc(aqua_ctx* ctx, NrcNet& net);

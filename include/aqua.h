@@ -294,14 +294,26 @@ AQUA_API aqua_status aqua_render(aqua_ctx* ctx, aqua_scene* scene,
                                  const aqua_integrator_cfg* cfg, const aqua_tuning* tuning,
                                  float* rgb_out, uint32_t flags, aqua_stats* stats);
 
-/* Times short renders over a grid of launch shapes and returns the fastest. */
+/* Times short renders (at most 16 spp) over a grid of launch shapes —
+ * material sort, traversal and shading block sizes, blocks per SM — and
+ * returns the fastest. The image does not depend on the choice. */
 AQUA_API aqua_status aqua_autotune(aqua_ctx* ctx, aqua_scene* scene,
                                    const aqua_integrator_cfg* cfg, aqua_tuning* out);
 
-/* Renders n jobs (uneven resolutions and spp, several scenes) in one
- * persistent launch. */
+/* Renders n jobs (views of up to n scenes, uneven resolutions and spp; at
+ * most 1024 jobs) in one persistent launch replayed from a captured CUDA
+ * graph (tuning->use_graph, on when tuning is NULL). Warps take work units
+ * of 32 pixels of one job from a global queue, in job order; each pixel's
+ * samples run in one lane, so every job's image equals aqua_render's with
+ * one slot per pixel. rgb_out of each job is a device buffer. stats->job_ms,
+ * when non-NULL, receives each job's completion time from the start of the
+ * launch (device clock). tuning->block_trace = threads per block (64, 128,
+ * 256), tuning->blocks_per_sm = persistent blocks per SM (0 = occupancy). */
 AQUA_API aqua_status aqua_render_batch(aqua_ctx* ctx, const aqua_job* jobs, size_t n,
                                        const aqua_tuning* tuning, aqua_batch_stats* stats);
+/* Times the batch's launch shapes on the same jobs at spp / 32 and returns
+ * the fastest (block size, blocks per SM). */
+AQUA_API aqua_status aqua_autotune_batch(aqua_ctx* ctx, const aqua_job* jobs, size_t n, aqua_tuning* out);
 
 /* Device memory currently held by the context's render workspace. */
 AQUA_API uint64_t aqua_workspace_bytes(const aqua_ctx* ctx);
