@@ -82,6 +82,24 @@ AQ_HD double dsub_rn(double a, double b) {
 }
 AQ_HD float fminf_(float a, float b) { return a < b ? a : b; }
 AQ_HD float fmaxf_(float a, float b) { return a > b ? a : b; }
+// Min/max of the slab test: one FMNMX on the device. The inputs are never
+// NaN (inverse directions are finite), so the result equals the
+// compare-select form except possibly for the sign of a zero, which no
+// comparison downstream can see.
+AQ_HD float smin(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return fminf(a, b);
+#else
+    return a < b ? a : b;
+#endif
+}
+AQ_HD float smax(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return fmaxf(a, b);
+#else
+    return a > b ? a : b;
+#endif
+}
 
 // ------------------------------------------------------------------ vectors
 struct v3 {
@@ -152,9 +170,12 @@ constexpr int kBounceDims = 8;  // light pick, light u/v, lobe, dir u/v, RR, spa
 
 // ------------------------------------------------------------------ ray/box
 // Slab test in the form (b - o) * invd (Ize 2013, "Robust BVH Ray Traversal",
-// JCGT 2(2)), with the far distance scaled by 1 + 2*gamma(3) so that a box the
-// exact ray touches is never rejected.
-constexpr float kSlabFarScale = 1.00000036f;  // 1 + 2*gamma_3, gamma_3 = 3u/(1-3u), u = 2^-24
+// JCGT 2(2)). The far distance is scaled by 1 + 1e-5, well above Ize's
+// 1 + 2*gamma(3) (3.6e-7): a box the exact ray touches is never rejected,
+// and a box is not culled by a triangle hit that ties with one inside it to
+// within the rounding of the triangle test either, so the closest hit, ties
+// broken by the smaller scene index, does not depend on the visit order.
+constexpr float kSlabFarScale = 1.00001f;
 
 struct RayPre {
     v3 o, invd;
@@ -174,8 +195,8 @@ AQ_HD float slab_entry(float lox, float hix, float loy, float hiy, float loz, fl
     float ty1 = mul_rn(sub_rn(hiy, r.o.y), r.invd.y);
     float tz0 = mul_rn(sub_rn(loz, r.o.z), r.invd.z);
     float tz1 = mul_rn(sub_rn(hiz, r.o.z), r.invd.z);
-    float tn = fmaxf_(fmaxf_(fminf_(tx0, tx1), fminf_(ty0, ty1)), fmaxf_(fminf_(tz0, tz1), r.tmin));
-    float tf = fminf_(fminf_(fmaxf_(tx0, tx1), fmaxf_(ty0, ty1)), fminf_(fmaxf_(tz0, tz1), tfar_limit));
+    float tn = smax(smax(smin(tx0, tx1), smin(ty0, ty1)), smax(smin(tz0, tz1), r.tmin));
+    float tf = smin(smin(smax(tx0, tx1), smax(ty0, ty1)), smin(smax(tz0, tz1), tfar_limit));
     tf = mul_rn(tf, kSlabFarScale);
     return tn <= tf ? tn : INFINITY;
 }

@@ -37,7 +37,6 @@ __device__ __forceinline__ unsigned long long device_clock_ns() {
 __device__ __forceinline__ void trace_path(const DevScene& S, const DevCamera& cam, uint64_t seed, uint32_t pixel,
                                            uint32_t sample, int max_depth, int rr_depth, const float* lut, v3& sum,
                                            uint32_t& n_ext, uint32_t& n_shadow) {
-    uint32_t dummy0 = 0, dummy1 = 0;
     uint64_t st = path_rng_state(seed, pixel, sample), inc = pixel_inc(pixel);
     float u0 = draw(st, inc), u1 = draw(st, inc), u2 = draw(st, inc), u3 = draw(st, inc);
     v3 o, dir;
@@ -46,7 +45,7 @@ __device__ __forceinline__ void trace_path(const DevScene& S, const DevCamera& c
     float pdf_b = 0.0f;
     for (int depth = 0;; ++depth) {
         ++n_ext;
-        TraceResult h = traverse<false, false>(S, o, dir, 0.0f, INFINITY, dummy0, dummy1);
+        TraceResult h = traverse_fast<false>(S, o, dir, 0.0f, INFINITY);
         if (h.tri < 0) {
             v3 e = mk(S.env[0], S.env[1], S.env[2]);
             if (e.x > 0.0f || e.y > 0.0f || e.z > 0.0f) sum = sum + thr * e;
@@ -134,7 +133,7 @@ __device__ __forceinline__ void trace_path(const DevScene& S, const DevCamera& c
             if (contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f) {
                 ++n_shadow;
                 v3 so = offset_ray(p, ng);
-                TraceResult sh = traverse<true, false>(S, so, wi, 0.0f, dist * (1.0f - 1e-4f), dummy0, dummy1);
+                TraceResult sh = traverse_fast<true>(S, so, wi, 0.0f, dist * (1.0f - 1e-4f));
                 if (sh.tri < 0) sum = sum + contrib;
             }
         }

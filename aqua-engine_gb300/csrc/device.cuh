@@ -125,6 +125,81 @@ __device__ __forceinline__ TraceResult traverse(const DevScene& S, v3 o, v3 d, f
     }
 }
 
+// Traversal with postponed leaves (Aila & Laine 2009, "Understanding the
+// Efficiency of Ray Traversal on GPUs"): a lane that reaches a leaf parks it
+// and keeps walking inner nodes until every lane of the warp still walking
+// holds a leaf (warp vote), then all test triangles together. Boxes, culling
+// and triangle tests are those of traverse(), so the result (the minimum
+// (t, scene index) over all triangles hit, or any hit) is identical; only
+// the order of visits, and thus the work counts, differ.
+constexpr int32_t kTraversalDone = (int32_t)0x80000000;
+
+template <bool ANY>
+__device__ __forceinline__ TraceResult traverse_fast(const DevScene& S, v3 o, v3 d, float tmin, float tmax) {
+    RayPre rp;
+    rp.o = o;
+    rp.invd = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+    rp.tmin = tmin;
+    rp.tmax = tmax;
+    RayShear sh = make_shear(o, d);
+    TraceResult r;
+    r.t = tmax; r.u = 0.0f; r.v = 0.0f; r.tri = -1; r.id = 0x7fffffff;
+    int32_t stack[kStackSize];
+    int sp = 0;
+    int32_t node = 0, leaf = 0;
+    while (true) {
+        while (node >= 0) {
+            const float4* np = S.nodes + 4 * (size_t)node;
+            float4 w0 = ldg_(np), w1 = ldg_(np + 1), w2 = ldg_(np + 2);
+            int4 w3 = ldg_(reinterpret_cast<const int4*>(np + 3));
+            float t0 = slab_entry(w0.x, w0.y, w0.z, w0.w, w2.x, w2.y, rp, r.t);
+            float t1 = slab_entry(w1.x, w1.y, w1.z, w1.w, w2.z, w2.w, rp, r.t);
+            bool h0 = t0 != INFINITY, h1 = t1 != INFINITY;
+            if (h0 && h1) {
+                bool swap = t1 < t0;
+                stack[sp++] = swap ? w3.x : w3.y;
+                node = swap ? w3.y : w3.x;
+            } else if (h0) {
+                node = w3.x;
+            } else if (h1) {
+                node = w3.y;
+            } else {
+                node = sp > 0 ? stack[--sp] : kTraversalDone;
+            }
+            if (node < 0 && node != kTraversalDone && leaf == 0) {
+                leaf = node;
+                node = sp > 0 ? stack[--sp] : kTraversalDone;
+            }
+            if (!__any_sync(__activemask(), leaf == 0)) break;
+        }
+        while (leaf < 0) {
+            int32_t code = ~leaf;
+            int32_t first = code >> 3, cnt = code & 7;
+            for (int k = 0; k < cnt; ++k) {
+                const float4* tp = S.tris + 3 * (size_t)(first + k);
+                float4 a = ldg_(tp), b = ldg_(tp + 1), c = ldg_(tp + 2);
+                TriHit h = intersect_tri(sh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), tmin, tmax);
+                if (h.hit) {
+                    int32_t id = __float_as_int(a.w);
+                    if (ANY) {
+                        r.t = h.t; r.tri = first + k; r.id = id;
+                        return r;
+                    }
+                    if (h.t < r.t || (h.t == r.t && id < r.id)) {
+                        r.t = h.t; r.u = h.u; r.v = h.v; r.tri = first + k; r.id = id;
+                    }
+                }
+            }
+            leaf = 0;
+            if (node < 0 && node != kTraversalDone) {
+                leaf = node;
+                node = sp > 0 ? stack[--sp] : kTraversalDone;
+            }
+        }
+        if (node == kTraversalDone) return r;
+    }
+}
+
 // Warp-aggregated append: lanes with pred set get consecutive slots of *ctr.
 __device__ __forceinline__ uint32_t warp_append(uint32_t* ctr, bool pred) {
     unsigned mask = __ballot_sync(__activemask(), pred);

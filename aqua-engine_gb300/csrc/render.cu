@@ -72,6 +72,9 @@ struct WavePtrs {
 
 // Counters of the cache mode (after the material buckets).
 enum { kCntQuery = 3, kCntRecord = 4, kCntTrainPath = 5 };
+// Dynamic-fetch cursors of the two traversal kernels; each kernel clears
+// the other's for the next launch.
+enum { kCntFetchTrace = 6, kCntFetchShadow = 7 };
 
 // ---------------------------------------------------------------- helpers
 
@@ -187,12 +190,23 @@ __global__ void __launch_bounds__(128) k_trace_ext(DevScene S, WaveParams P, Wav
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counters[cnt_out] = 0;
         W.counters[kCntShadow] = 0;
+        W.counters[kCntFetchShadow] = 0;
     }
+    const int lane_id = threadIdx.x & 31;
     uint32_t nodes = 0, tris = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    // Each warp takes the next 32 rays of the queue (dynamic fetch: warps
+    // whose rays finish early take more).
+    while (true) {
+        uint32_t base = 0;
+        if (lane_id == 0) base = atomicAdd(&W.counters[kCntFetchTrace], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + (uint32_t)lane_id;
+        if (i >= n) continue;
         uint32_t s = W.q_in[i];
         float4 ro = W.ray_o[s], rd = W.ray_d[s];
-        TraceResult r = traverse<false, COUNT>(S, f3(ro), f3(rd), ro.w, rd.w, nodes, tris);
+        TraceResult r = COUNT ? traverse<false, true>(S, f3(ro), f3(rd), ro.w, rd.w, nodes, tris)
+                              : traverse_fast<false>(S, f3(ro), f3(rd), ro.w, rd.w);
         W.hit[s] = make_float4(r.t, r.u, r.v, __int_as_float(r.tri));
         if (SORTED) {
             uint32_t b = r.tri < 0 ? P.nb - 1
@@ -225,7 +239,7 @@ __global__ void __launch_bounds__(128) k_trace_ext(DevScene S, WaveParams P, Wav
 // so far) so that the radiance leaving each of their vertices becomes a
 // training target once the path is complete.
 template <bool SORTED, bool NRC = false>
-__global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtrs W, uint32_t cnt_in,
+__global__ void __launch_bounds__(128, 8) k_shade(DevScene S, WaveParams P, WavePtrs W, uint32_t cnt_in,
                                                uint32_t cnt_out) {
     __shared__ float lut[256];
     __shared__ uint32_t prefix[257];
@@ -442,12 +456,22 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, WaveParams P, WavePtr
 template <bool COUNT, bool NRC = false>
 __global__ void __launch_bounds__(128) k_shadow(DevScene S, WaveParams P, WavePtrs W) {
     uint32_t n = W.counters[kCntShadow];
-    if (blockIdx.x == 0)
+    if (blockIdx.x == 0) {
         for (uint32_t b = threadIdx.x; b < P.nb; b += blockDim.x) W.counters[kCntBucket0 + b] = 0;
+        if (threadIdx.x == 0) W.counters[kCntFetchTrace] = 0;
+    }
+    const int lane_id = threadIdx.x & 31;
     uint32_t nodes = 0, tris = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    while (true) {
+        uint32_t base = 0;
+        if (lane_id == 0) base = atomicAdd(&W.counters[kCntFetchShadow], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + (uint32_t)lane_id;
+        if (i >= n) continue;
         float4 o = W.sh_o[i], d = W.sh_d[i];
-        TraceResult r = traverse<true, COUNT>(S, f3(o), f3(d), 0.0f, d.w, nodes, tris);
+        TraceResult r = COUNT ? traverse<true, true>(S, f3(o), f3(d), 0.0f, d.w, nodes, tris)
+                              : traverse_fast<true>(S, f3(o), f3(d), 0.0f, d.w);
         if (r.tri < 0) {
             float4 c = W.sh_c[i];
             if (!(NRC && P.visualize)) film_add(W.film, (uint32_t)__float_as_int(o.w), mk(c.x, c.y, c.z));

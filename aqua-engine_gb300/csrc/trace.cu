@@ -14,7 +14,8 @@ __global__ void __launch_bounds__(128) k_trace_user(DevScene S, const float4* __
     uint32_t nodes = 0, tris = 0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         float4 a = ldg_(rays + 2 * i), b = ldg_(rays + 2 * i + 1);
-        TraceResult r = traverse<ANY, COUNT>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, nodes, tris);
+        TraceResult r = COUNT ? traverse<ANY, true>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, nodes, tris)
+                              : traverse_fast<ANY>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w);
         float4 h;
         if (ANY) h = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(r.tri >= 0 ? 1 : -1));
         else if (r.tri < 0) h = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));

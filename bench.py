@@ -269,6 +269,52 @@ def run_nrc_metric(ctx, budget_s: float = 60.0, overrides: dict | None = None):
     return out
 
 
+BATCH_WORKLOAD = {"workload": "batch-64-jobs-4-scenes",
+                  "scenes": ["Cornell Lambert (36 tris)", "Cornell GGX (36 tris)",
+                             "synthetic interior (1.15M tris, 8 textures)", "random-sphere field (4.0M tris)"],
+                  "jobs": 64, "resolutions": [128, 256, 512, 1024], "spp_range": [16, 1024],
+                  "spp_distribution": "log-uniform, seed 5", "max_depth": 8}
+
+
+def run_batch_metric(ctx, warmup: int = 1, steps: int = 2):
+    """64 jobs over 4 seeded scenes in one persistent launch per step:
+    aggregate Mpaths/s and per-job completion latency p50/p99."""
+    import numpy as np
+    import torch
+
+    W = BATCH_WORKLOAD
+    t0 = time.perf_counter()
+    scenes = [ctx.procedural(c, seed=0) for c in (1, 2, 3, 5)]
+    t_scenes = time.perf_counter() - t0
+    rng = np.random.default_rng(5)
+    specs = []
+    for i in range(W["jobs"]):
+        res = int(rng.choice(W["resolutions"]))
+        spp = int(round(np.exp(rng.uniform(np.log(16), np.log(1024)))))
+        specs.append((int(rng.integers(0, 4)), res, res, spp, W["max_depth"], 1000 + i))
+    bufs = [torch.empty(r * r * 3, dtype=torch.float32, device="cuda") for (_, r, _, _, _, _) in specs]
+    jobs = [(scenes[s], w, h, spp, d, seed, b.data_ptr()) for (s, w, h, spp, d, seed), b in zip(specs, bufs)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tune = ctx.autotune_batch(jobs)
+    t_tune = time.perf_counter() - t0
+    for _ in range(warmup):
+        ctx.render_batch(jobs, tune)
+    ms, paths, lat = 0.0, 0, []
+    for _ in range(steps):
+        st, job_ms = ctx.render_batch(jobs, tune)
+        ms += st.device_ms
+        paths += st.paths
+        lat.extend(job_ms.tolist())
+    for s in scenes:
+        s.free()
+    return {"config": W, "value": paths / (ms * 1e-3) / 1e6, "unit": "Mpaths/s", "ms_per_batch": ms / steps,
+            "paths_per_batch": paths // steps, "job_latency_ms": {"p50": float(np.percentile(lat, 50)),
+                                                                   "p99": float(np.percentile(lat, 99))},
+            "tuning": {"block": tune.block_trace, "blocks_per_sm": tune.blocks_per_sm, "graph": tune.use_graph},
+            "autotune_s": round(t_tune, 2), "scene_build_s": round(t_scenes, 2), "steps": steps, "warmup": warmup}
+
+
 def run_reference(args, world, rank, pg):
     if rank != 0:
         return
@@ -377,6 +423,9 @@ def run_gpu(args, world, rank, local, pg):
     nrc = None
     if rank == 0 and not args.no_nrc:
         nrc = run_nrc_metric(ctx, args.nrc_budget)
+    batch = None
+    if rank == 0 and not args.no_batch:
+        batch = run_batch_metric(ctx)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -400,6 +449,7 @@ def run_gpu(args, world, rank, local, pg):
                         "d2h_bytes_per_step": int(info.width * info.height * 12)},
                 "gpu_launches": gpu_launches,
                 "nrc_time_to_relmse": nrc,
+                "batch": batch,
                 "stage_ms_per_step": {"trace": trace_ms / args.steps,
                                       "shade": sum(s.shade_ms for s in steps) / args.steps,
                                       "shadow": sum(s.shadow_ms for s in steps) / args.steps}}
@@ -418,6 +468,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-nrc", action="store_true", help="skip the cached-vs-plain time-to-relMSE measurement")
     ap.add_argument("--nrc-budget", type=float, default=60.0, help="seconds per arm of that measurement")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-job batched-serving measurement")
     ap.add_argument("--traffic-per-launch", type=float, default=None,
                     help="DRAM bytes per k_trace_ext launch from an ncu capture")
     ap.add_argument("--spp", type=int, default=0,

@@ -174,7 +174,7 @@ inline float entry_f(const float* lo_hi_xy, float loz, float hiz, const RayF& r,
     float tz0 = (loz - r.o.z) * r.invd.z, tz1 = (hiz - r.o.z) * r.invd.z;
     float tn = mx(mx(mn(tx0, tx1), mn(ty0, ty1)), mx(mn(tz0, tz1), r.tmin));
     float tf = mn(mn(mx(tx0, tx1), mx(ty0, ty1)), mn(mx(tz0, tz1), tlim));
-    tf = tf * 1.00000036f;
+    tf = tf * 1.00001f;  // conservative far scale, 1e-5 relative
     return tn <= tf ? tn : std::numeric_limits<float>::infinity();
 }
 
