@@ -145,12 +145,13 @@ def cpu_sample_run(threads: int, target_s: float, seed: int = 0):
     orc = pyoracle.OracleScene.from_aqua(scene)
     W = WORKLOAD["width"]
     mid = (WORKLOAD["height"] // 2) * W
-    # calibrate on 64 pixels, then size the band for ~target_s seconds
+    # calibrate on 2048 pixels (32 chunks of 64 for the thread pool), then
+    # size the band for ~target_s seconds
     t0 = time.perf_counter()
     orc.render(WORKLOAD["spp"], WORKLOAD["max_depth"], seed=seed, precision=32, rr_depth=WORKLOAD["rr_depth"],
-               threads=threads, pixel_begin=mid, pixel_end=mid + 64)
+               threads=threads, pixel_begin=mid, pixel_end=mid + 2048)
     dt = max(time.perf_counter() - t0, 1e-3)
-    npx = int(max(64, min(W * 64, 64 * target_s / dt)))
+    npx = int(max(2048, min(W * 256, 2048 * target_s / dt)))
     t0 = time.perf_counter()
     _, st = orc.render(WORKLOAD["spp"], WORKLOAD["max_depth"], seed=seed, precision=32,
                        rr_depth=WORKLOAD["rr_depth"], threads=threads, pixel_begin=mid, pixel_end=mid + npx)
@@ -267,6 +268,62 @@ def run_nrc_metric(ctx, budget_s: float = 60.0, overrides: dict | None = None):
            "time_ratio_cached_over_plain": (t_cached / t_plain) if (t_cached and t_plain) else None,
            "budget_s": budget_s}
     return out
+
+
+def measure_l2_copy_gbs(device: int) -> dict:
+    """L2-resident copy bandwidth: two buffers that fit in the 129 MB L2
+    copied back and forth (read + write bytes), best of 20, CUDA events."""
+    import torch
+
+    best = {}
+    for mb in (8, 16, 32):
+        n = mb * (1 << 20) // 2
+        a = torch.ones(n, dtype=torch.bfloat16, device=f"cuda:{device}")
+        b = torch.empty_like(a)
+        for _ in range(5):
+            b.copy_(a)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(20):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(10):
+                b.copy_(a)
+                a.copy_(b)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+        best[mb] = 20 * 2 * a.numel() * 2 / min(times) / 1e9
+    return {"gbs": max(best.values()), "by_buffer_mb": best}
+
+
+INTERIOR_WORKLOAD = {"workload": "interior-1920x1080-256spp-depth8", "width": 1920, "height": 1080, "spp": 256,
+                     "max_depth": 8, "scene": "synthetic interior: 153 meshes, 1.15M triangles, 8 textures, "
+                                              "16 quad lights, seed 0"}
+
+
+def run_interior_metric(ctx, warmup: int = 1, steps: int = 2):
+    """Plain path tracing of the interior at 1080p, 256 spp (one step = the
+    whole image)."""
+    import torch
+    import aqua
+
+    W = INTERIOR_WORKLOAD
+    scene = ctx.procedural(3, seed=0, width=W["width"], height=W["height"])
+    film = torch.zeros(W["width"] * W["height"] * 3, dtype=torch.float32, device="cuda")
+    cfg = ctx.integrator(spp=W["spp"], max_depth=W["max_depth"], rr_depth=3, seed=1)
+    torch.cuda.synchronize()
+    for _ in range(warmup):
+        ctx.render_device(scene, cfg, film.data_ptr())
+    ms, paths, rays = 0.0, 0, 0
+    for _ in range(steps):
+        st = ctx.render_device(scene, cfg, film.data_ptr())
+        ms += st.device_ms
+        paths += st.paths
+        rays += st.ext_rays + st.shadow_rays
+    scene.free()
+    return {"config": W, "value": paths / (ms * 1e-3) / 1e6, "unit": "Mpaths/s", "mrays_per_s": rays / (ms * 1e-3) / 1e6,
+            "ms_per_step": ms / steps, "steps": steps, "warmup": warmup}
 
 
 BATCH_WORKLOAD = {"workload": "batch-64-jobs-4-scenes",
@@ -420,6 +477,10 @@ def run_gpu(args, world, rank, local, pg):
     e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
     e2e_value = sum_over_ranks(pg, e2e_paths) / e2e_s / 1e6
 
+    l2 = measure_l2_copy_gbs(local)
+    roofline["l2_copy_gbs"] = l2["gbs"]
+    roofline["frac_of_l2_copy"] = achieved / l2["gbs"]
+    interior = run_interior_metric(ctx) if rank == 0 and not args.no_interior else None
     nrc = None
     if rank == 0 and not args.no_nrc:
         nrc = run_nrc_metric(ctx, args.nrc_budget)
@@ -448,6 +509,7 @@ def run_gpu(args, world, rank, local, pg):
                 "e2e": {"value": e2e_value, "unit": "Mpaths/s", "h2d_bytes_per_step": int(info.upload_bytes),
                         "d2h_bytes_per_step": int(info.width * info.height * 12)},
                 "gpu_launches": gpu_launches,
+                "interior": interior,
                 "nrc_time_to_relmse": nrc,
                 "batch": batch,
                 "stage_ms_per_step": {"trace": trace_ms / args.steps,
@@ -469,7 +531,12 @@ def main():
     ap.add_argument("--no-nrc", action="store_true", help="skip the cached-vs-plain time-to-relMSE measurement")
     ap.add_argument("--nrc-budget", type=float, default=60.0, help="seconds per arm of that measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-job batched-serving measurement")
-    ap.add_argument("--traffic-per-launch", type=float, default=None,
+    ap.add_argument("--no-interior", action="store_true", help="skip the 1080p interior measurement")
+    # dram__bytes_read.sum + dram__bytes_write.sum of one full-queue
+    # k_trace_ext launch (1M rays) of this workload, from `ncu --set full`
+    # (41.04 MB read + 3.55 MB written); every launch of the step has the
+    # same queue size until the last samples drain.
+    ap.add_argument("--traffic-per-launch", type=float, default=44.59e6,
                     help="DRAM bytes per k_trace_ext launch from an ncu capture")
     ap.add_argument("--spp", type=int, default=0,
                     help="samples per pixel of the workload (default 1024; smaller only for profiling captures)")
