@@ -173,7 +173,10 @@ NRC_PARAMS = 20672
 class NrcCfg(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
                 ("seed", C.c_uint64), ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3),
-                ("ema_decay", C.c_float)]
+                ("ema_decay", C.c_float), ("forward_kernel", C.c_int32)]
+
+
+NRC_KERNEL_AUTO, NRC_KERNEL_MMA_SYNC, NRC_KERNEL_TCGEN05 = 0, 1, 2
 
 
 class Nrc:

@@ -640,6 +640,9 @@ AQUA_API aqua_status aqua_nrc_create(aqua_ctx* ctx, const aqua_nrc_cfg* cfg, aqu
             n->net.eps = c.eps;
             need(c.ema_decay >= 0.0f && c.ema_decay < 1.0f, "ema_decay must be in [0, 1)");
             n->net.ema_decay = c.ema_decay;
+            need(c.forward_kernel >= AQUA_NRC_KERNEL_AUTO && c.forward_kernel <= AQUA_NRC_KERNEL_TCGEN05,
+                 "forward_kernel must be an AQUA_NRC_KERNEL_* value");
+            n->net.forward_tc = c.forward_kernel != AQUA_NRC_KERNEL_MMA_SYNC;
             for (int i = 0; i < 3; ++i) {
                 n->net.bmin[i] = c.bbox_min[i];
                 n->net.bext[i] = c.bbox_max[i] - c.bbox_min[i];
@@ -735,6 +738,7 @@ AQUA_API aqua_status aqua_nrc_forward(aqua_ctx* ctx, aqua_nrc* n, const uint16_t
         if (!(flags & AQUA_NRC_DEVICE_PTRS))
             AQ_CUDA(cudaMemcpyAsync(out, d_out, 12 * cnt, cudaMemcpyDeviceToHost, ctx->stream));
         AQ_CUDA(cudaStreamSynchronize(ctx->stream));
+        nrc_check_tc(ctx, n->net);
     });
 }
 

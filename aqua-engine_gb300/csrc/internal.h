@@ -71,6 +71,9 @@ struct NrcNet {
     double* loss = nullptr;  // loss sum of the last step
     float* ema = nullptr;    // exponential moving average of w (inference weights)
     uint2* frag_inf = nullptr;  // forward fragments of the inference weights
+    uint8_t* img_tc = nullptr;  // inference weights in the tcgen05 shared-memory layout
+    uint32_t* tc_err = nullptr; // set by the tcgen05 kernel when a wait expired
+    int forward_tc = 0;         // 1: inference runs on tcgen05 (else mma.sync)
     float ema_decay = 0.0f;  // 0 = inference uses w itself
     DevBuf train;            // training scratch, sized by train_rows
     int train_rows = 0;
@@ -204,6 +207,12 @@ void nrc_pack(aqua_ctx* ctx, NrcNet& net);
 void nrc_forward_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, int n, float* out);
 void nrc_train_step_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, const float* target, int n);
 void nrc_encode_dev(aqua_ctx* ctx, NrcNet& net, const float* raw, int n, uint16_t* X);
+// tcgen05 inference (nrc_tc.cu)
+size_t nrc_tc_weight_bytes();
+void nrc_pack_tc(aqua_ctx* ctx, const float* w, void* img);
+void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n, float* out, uint32_t* err);
+// Throws when a tcgen05 launch since the last check gave up waiting (syncs the stream).
+void nrc_check_tc(aqua_ctx* ctx, NrcNet& net);
 
 // Render on the library's fixed static scratch array; no device allocation.
 void render_noalloc(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg& cfg, float* rgb_out,

@@ -355,7 +355,8 @@ void nrc_alloc(aqua_ctx* ctx, NrcNet& net) {
     auto take = [&](size_t b) { size_t o = off; off = rup(off + b, 256); return o; };
     size_t o_w = take(4 * kNrcParams), o_m = take(4 * kNrcParams), o_v = take(4 * kNrcParams),
            o_g = take(4 * kNrcParams), o_f = take(8 * kFragFwd), o_b = take(8 * kFragBwd), o_l = take(64),
-           o_e = take(4 * kNrcParams), o_fi = take(8 * kFragFwd);
+           o_e = take(4 * kNrcParams), o_fi = take(8 * kFragFwd), o_tc = take(nrc_tc_weight_bytes()),
+           o_er = take(4);
     dev_alloc(ctx, net.block, off);
     char* b = (char*)net.block.ptr;
     net.w = (float*)(b + o_w);
@@ -367,6 +368,9 @@ void nrc_alloc(aqua_ctx* ctx, NrcNet& net) {
     net.loss = (double*)(b + o_l);
     net.ema = (float*)(b + o_e);
     net.frag_inf = (uint2*)(b + o_fi);
+    net.img_tc = (uint8_t*)(b + o_tc);
+    net.tc_err = (uint32_t*)(b + o_er);
+    AQ_CUDA(cudaMemsetAsync(net.tc_err, 0, 4, ctx->stream));
 }
 
 void nrc_release(NrcNet& net) {
@@ -392,9 +396,10 @@ void nrc_pack(aqua_ctx* ctx, NrcNet& net) {
     int total = kFragFwd + kFragBwd;
     k_nrc_pack<<<(total + 255) / 256, 256, 0, ctx->stream>>>(net.w, net.frag, net.fragT);
     // Forward fragments of the inference weights (the EMA when enabled).
-    k_nrc_pack<<<(kFragFwd + 255) / 256, 256, 0, ctx->stream>>>(net.ema_decay > 0.0f ? net.ema : net.w,
-                                                               net.frag_inf, nullptr);
+    const float* inf = net.ema_decay > 0.0f ? net.ema : net.w;
+    k_nrc_pack<<<(kFragFwd + 255) / 256, 256, 0, ctx->stream>>>(inf, net.frag_inf, nullptr);
     AQ_CUDA(cudaGetLastError());
+    if (net.forward_tc) nrc_pack_tc(ctx, inf, net.img_tc);
 }
 
 void nrc_set_weights(aqua_ctx* ctx, NrcNet& net, const float* host_w) {
@@ -416,6 +421,10 @@ static int nrc_grid(aqua_ctx* ctx, int rows) {
 
 void nrc_forward_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, int n, float* out) {
     if (n <= 0) return;
+    if (net.forward_tc) {
+        nrc_forward_tc_dev(ctx, net.img_tc, X, n, out, net.tc_err);
+        return;
+    }
     k_nrc_forward<false><<<nrc_grid(ctx, n), 128, 0, ctx->stream>>>(reinterpret_cast<const uint32_t*>(X), n,
                                                                      net.frag_inf, out, nullptr);
     AQ_CUDA(cudaGetLastError());
@@ -460,6 +469,17 @@ void nrc_train_step_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, const flo
     nrc_pack(ctx, net);
     AQ_CUDA(cudaGetLastError());
     net.launches += 5;
+}
+
+void nrc_check_tc(aqua_ctx* ctx, NrcNet& net) {
+    if (!net.forward_tc) return;
+    uint32_t e = 0;
+    AQ_CUDA(cudaMemcpyAsync(&e, net.tc_err, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    AQ_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (e) {
+        AQ_CUDA(cudaMemsetAsync(net.tc_err, 0, 4, ctx->stream));
+        throw Error(AQUA_ERR_TIMEOUT, "tensor-core inference: an MMA completion wait expired");
+    }
 }
 
 void nrc_encode_dev(aqua_ctx* ctx, NrcNet& net, const float* raw, int n, uint16_t* X) {

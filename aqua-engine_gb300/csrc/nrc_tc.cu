@@ -1,0 +1,400 @@
+// nrc_tc.cu — radiance-cache inference on the 5th-generation tensor cores:
+// tcgen05.mma with the accumulator in tensor memory (TMEM), inputs brought in
+// by TMA.
+//
+// One persistent CTA per SM holds the network's bf16 weights (42 KB) in shared
+// memory once and runs kTcGroups independent warpgroups. A warpgroup owns 128
+// TMEM columns (64 for the FP32 accumulator, 32 for the next layer's bf16
+// activations) and a 128-row input tile in shared memory, and works through
+// its tiles alone:
+//   - its first thread loads the next input tile with TMA (eight 128 x 8-column
+//     boxes) as soon as layer 1 has read the current one;
+//   - per layer the same thread issues four tcgen05.mma.kind::f16 (M = 128,
+//     N = 64, or 16 for the output layer, K = 16 each; BF16 x BF16 -> FP32)
+//     and commits them to the group's mbarrier. Layer 1 reads A from shared
+//     memory, layers 2-6 read it from TMEM;
+//   - each warp reads its 32 TMEM lanes (rows) of the accumulator with
+//     tcgen05.ld, applies ReLU, rounds to bf16 pairs and stores them back to
+//     the activation columns with tcgen05.st.
+// Activations never leave TMEM, and while one group is in its epilogue the
+// tensor core serves the others.
+//
+// Shared-memory operands use the K-major layout without swizzle, with the
+// 8-row x 16-byte core matrices of one 8-column K slice stored back to back:
+// element (r, k) of an R-row tile sits at (k / 8) * R * 16 + r * 16 + (k % 8) * 2.
+// So the leading byte offset (next core matrix along K) is R * 16 and the
+// stride byte offset (next 8 rows) is 128, and a TMA box of 8 columns x 128
+// rows lands as one contiguous K slice.
+//
+// Every mbarrier wait is bounded. A group whose wait expires agrees on it
+// with a barrier reduction, records an error flag, waits (bounded) for what
+// it still has in flight and leaves; TMEM is freed on every path.
+#include <algorithm>
+#include <mutex>
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include "internal.h"
+#include "nrc.h"
+
+namespace aq {
+
+constexpr int kTcRows = 128;                      // rows per tile (MMA M)
+constexpr int kTcGroups = 4;                      // warpgroups (tiles in flight) per CTA
+constexpr int kTcThreads = 128 * kTcGroups;
+constexpr int kTcTileBytes = kTcRows * 64 * 2;    // 16 KB per input or activation tile
+constexpr int kTcLayerBytes = 64 * 64 * 2;        // 8 KB hidden-layer weights
+constexpr int kTcOutRows = 16;                    // output layer padded to N = 16 (3 used)
+constexpr int kTcOutBytes = kTcOutRows * 64 * 2;  // 2 KB
+constexpr int kTcWeightBytes = 5 * kTcLayerBytes + kTcOutBytes;  // 42 KB
+// The input tiles need 106 KB; asking for 120 KB keeps two CTAs (and two
+// full TMEM allocations) off one SM.
+constexpr int kTcSmemBytes = std::max(kTcWeightBytes + kTcGroups * kTcTileBytes + 1024, 120 * 1024);
+constexpr uint32_t kTcGroupCols = 128;            // accumulator 64 + activations 32, rounded up
+constexpr uint32_t kTcActCol = 64;                // activation columns within a group
+constexpr uint32_t kTcTmemCols = kTcGroupCols * kTcGroups;  // a power of two >= 32
+constexpr uint32_t kTcWaitLimit = 1u << 22;       // try_wait rounds before a wait gives up
+static_assert((kTcTmemCols & (kTcTmemCols - 1)) == 0 && kTcTmemCols >= 32 && kTcTmemCols <= 512, "TMEM alloc");
+static_assert(kTcWeightBytes % 1024 == 0 && kTcTileBytes % 1024 == 0, "tiles stay 1024-byte aligned");
+static_assert(kTcSmemBytes <= 227 * 1024, "shared memory per CTA");
+
+// Byte offset of element (r, k) in an R-row operand tile.
+__host__ __device__ constexpr uint32_t tc_offset(int rows, int r, int k) {
+    return (uint32_t)((k >> 3) * rows * 16 + r * 16 + (k & 7) * 2);
+}
+
+// Weights (rows = outputs, K = inputs) into the operand layout, bf16:
+// W1..W5 (64 rows each) then W6 padded to 16 rows.
+__global__ void k_nrc_pack_tc(const float* __restrict__ w, uint8_t* __restrict__ img) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;  // one element
+    const int hidden = 5 * 64 * 64;
+    if (i < hidden) {
+        int l = i / 4096, r = (i / 64) % 64, k = i % 64;
+        *reinterpret_cast<__nv_bfloat16*>(img + l * kTcLayerBytes + tc_offset(64, r, k)) = __float2bfloat16_rn(w[i]);
+    } else if (i < hidden + kTcOutRows * 64) {
+        int j = i - hidden, r = j / 64, k = j % 64;
+        float x = r < kNrcOut ? w[hidden + r * 64 + k] : 0.0f;
+        *reinterpret_cast<__nv_bfloat16*>(img + 5 * kTcLayerBytes + tc_offset(kTcOutRows, r, k)) =
+            __float2bfloat16_rn(x);
+    }
+}
+
+// ---------------------------------------------------------------- PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: start address, leading byte offset (next
+// core matrix along K), stride byte offset (next 8 rows), all >> 4; bit 46 =
+// descriptor version 1; swizzle none.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)(128u >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor, kind::f16: D = F32 (bits 4-5), A = B = BF16 (bits
+// 7-9, 10-12), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "setp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+        "}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+// Same with A (128 rows x 16 bf16, two per 32-bit column) read from TMEM.
+__device__ __forceinline__ void tc_mma_ts(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "setp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n"
+        "}\n" ::"r"(tmem_d),
+        "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+                 : "memory");
+}
+
+// Bounded wait on an mbarrier phase; false when the limit expired.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (uint32_t it = 0; it < kTcWaitLimit; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n"
+            ".reg .pred p;\n"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n"
+            "}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Barrier over one warpgroup (named barrier `id`, 128 threads) that also
+// returns whether any of its threads passed `pred`.
+__device__ __forceinline__ bool group_any(int id, bool pred) {
+    uint32_t r;
+    asm volatile(
+        "{\n"
+        ".reg .pred p, q;\n"
+        "setp.ne.u32 p, %1, 0;\n"
+        "bar.red.or.pred q, %2, 128, p;\n"
+        "selp.u32 %0, 1, 0, q;\n"
+        "}\n"
+        : "=r"(r)
+        : "r"((uint32_t)pred), "r"(id)
+        : "memory");
+    return r != 0;
+}
+
+// One input tile: eight boxes of 8 columns x 128 rows, 16 KB on one mbarrier.
+__device__ __forceinline__ void tma_load_tile(const CUtensorMap* map, uint32_t dst, uint32_t mbar, int row0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"((uint32_t)kTcTileBytes)
+                 : "memory");
+#pragma unroll
+    for (int kc = 0; kc < 8; ++kc)
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+                dst + (uint32_t)(kc * kTcRows * 16)),
+            "l"(reinterpret_cast<uint64_t>(map)), "r"(kc * 8), "r"(row0), "r"(mbar)
+            : "memory");
+}
+
+#define AQ_TC_LD16(taddr, r)                                                                               \
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, " \
+                 "[%16];\n"                                                                                \
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),     \
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), \
+                   "=r"(r[14]), "=r"(r[15])                                                                \
+                 : "r"(taddr))
+
+#define AQ_TC_ST16(taddr, r)                                                                               \
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "                                          \
+                 "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(taddr),              \
+                 "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),    \
+                 "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]) \
+                 : "memory")
+
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// ReLU and round-to-nearest-even to a bf16 pair: `lo` (the even K index) in
+// the low half, `hi` in the high half.
+__device__ __forceinline__ uint32_t relu_pack2(uint32_t lo, uint32_t hi) {
+    uint32_t d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;\n" : "=r"(d) : "f"(__uint_as_float(hi)), "f"(__uint_as_float(lo)));
+    return d;
+}
+
+// ---------------------------------------------------------------- kernel
+// X (through `xmap`): n rows x 64 bf16; out: n x 3 fp32; err: set to 1 when a
+// wait expired.
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_nrc_forward_tc(const __grid_constant__ CUtensorMap xmap, int n, const uint4* __restrict__ wimg,
+                     float* __restrict__ out, uint32_t* __restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t bar_in[kTcGroups], bar_mma[kTcGroups];
+    __shared__ uint32_t tmem_base_slot;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int g = warp >> 2, q = warp & 3, gt = tid & 127;
+    const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    uint8_t* sbase = smem_raw + (base - smem_u32(smem_raw));
+    const uint32_t sW = base;
+    const uint32_t sI = base + kTcWeightBytes + (uint32_t)g * kTcTileBytes;  // this group's input tile
+
+    for (int i = tid; i < kTcWeightBytes / 16; i += kTcThreads) reinterpret_cast<uint4*>(sbase)[i] = wimg[i];
+    if (tid < kTcGroups) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar_in[tid])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar_mma[tid])) : "memory");
+    }
+    if (tid == 0) {
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&xmap)) : "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         smem_u32(&tmem_base_slot)),
+                     "r"(kTcTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+
+    const uint32_t tmem = tmem_base_slot + (uint32_t)g * kTcGroupCols;   // this group's accumulator
+    const uint32_t tact = tmem + kTcActCol;                              // and activations
+    const uint32_t lanes = (uint32_t)(q * 32) << 16;                     // this warp's lanes
+    const uint32_t mb_in = smem_u32(&bar_in[g]), mb_mma = smem_u32(&bar_mma[g]);
+    const int bar_id = 1 + g;
+    const int tiles = (n + kTcRows - 1) / kTcRows;
+    const int stride = (int)gridDim.x * kTcGroups;
+    const int row = q * 32 + lane;  // TMEM lane = tile row
+    uint32_t ph_in = 0, ph_mma = 0;      // parity of the next phase to wait for
+    uint32_t tma_par = 0, mma_par = 0;   // parity the work in flight will complete
+    bool fail = false, tma_pending = false, mma_pending = false;
+
+    int tile = (int)blockIdx.x * kTcGroups + g;
+    if (gt == 0 && tile < tiles) {
+        tma_load_tile(&xmap, sI, mb_in, tile * kTcRows);
+        tma_pending = true;
+        tma_par = ph_in;
+    }
+    while (tile < tiles) {
+        bool ok = true;
+        if (gt == 0) {
+            ok = mbar_wait(mb_in, ph_in);
+            if (ok) tma_pending = false;
+        }
+        ph_in ^= 1u;
+        if (group_any(bar_id, !ok)) { fail = true; break; }
+        const int next = tile + stride;
+        for (int l = 0; l < 6; ++l) {
+            const bool last = l == 5;
+            if (gt == 0) {
+                tc_fence_after();
+                const uint32_t idesc = tc_idesc(kTcRows, last ? kTcOutRows : 64);
+                const uint32_t b0 = sW + (uint32_t)l * kTcLayerBytes;
+                const uint32_t blbo = (last ? kTcOutRows : 64) * 16;
+                // K = 64 as four K = 16 steps: two core matrices of B each, and
+                // of A two core matrices (layer 1) or eight TMEM columns.
+                if (l == 0) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        tc_mma(tmem, tc_desc(sI + (uint32_t)k * 2u * (kTcRows * 16), kTcRows * 16),
+                               tc_desc(b0 + (uint32_t)k * 2u * blbo, blbo), idesc, k > 0 ? 1u : 0u);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        tc_mma_ts(tmem, tact + (uint32_t)k * 8u, tc_desc(b0 + (uint32_t)k * 2u * blbo, blbo), idesc,
+                                  k > 0 ? 1u : 0u);
+                }
+                tc_commit(mb_mma);
+                mma_pending = true;
+                mma_par = ph_mma;
+            }
+            ok = mbar_wait(mb_mma, ph_mma);
+            ph_mma ^= 1u;
+            ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld below is warp-collective
+            if (gt == 0 && ok) mma_pending = false;
+            // The input tile is free once layer 1 has read it: fetch the next one.
+            if (l == 0 && gt == 0 && ok && next < tiles) {
+                tma_load_tile(&xmap, sI, mb_in, next * kTcRows);
+                tma_pending = true;
+                tma_par = ph_in;
+            }
+            tc_fence_after();
+            if (ok) {
+                if (!last) {
+                    uint32_t r[64], a[32];
+                    AQ_TC_LD16(tmem + lanes + 0u, (r + 0));
+                    AQ_TC_LD16(tmem + lanes + 16u, (r + 16));
+                    AQ_TC_LD16(tmem + lanes + 32u, (r + 32));
+                    AQ_TC_LD16(tmem + lanes + 48u, (r + 48));
+                    tc_wait_ld();
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) a[c] = relu_pack2(r[2 * c], r[2 * c + 1]);
+                    AQ_TC_ST16(tact + lanes + 0u, (a + 0));
+                    AQ_TC_ST16(tact + lanes + 16u, (a + 16));
+                    tc_wait_st();
+                } else {
+                    uint32_t r[16];
+                    AQ_TC_LD16(tmem + lanes, r);
+                    tc_wait_ld();
+                    const int grow = tile * kTcRows + row;
+                    if (grow < n) {
+                        out[(size_t)grow * 3 + 0] = __uint_as_float(r[0]);
+                        out[(size_t)grow * 3 + 1] = __uint_as_float(r[1]);
+                        out[(size_t)grow * 3 + 2] = __uint_as_float(r[2]);
+                    }
+                }
+            }
+            tc_fence_before();
+            if (group_any(bar_id, !ok)) { fail = true; break; }
+        }
+        if (fail) break;
+        tile = next;
+    }
+    if (fail && gt == 0) {
+        atomicExch(err, 1u);
+        // Let what this group still has in flight land (bounded) before TMEM is freed.
+        if (mma_pending) mbar_wait(mb_mma, mma_par);
+        if (tma_pending) mbar_wait(mb_in, tma_par);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem_base_slot),
+                     "r"(kTcTmemCols)
+                     : "memory");
+    }
+}
+
+// ---------------------------------------------------------------- host side
+size_t nrc_tc_weight_bytes() { return (size_t)kTcWeightBytes; }
+
+void nrc_pack_tc(aqua_ctx* ctx, const float* w, void* img) {
+    int total = 5 * 4096 + kTcOutRows * 64;
+    k_nrc_pack_tc<<<(total + 255) / 256, 256, 0, ctx->stream>>>(w, (uint8_t*)img);
+    AQ_CUDA(cudaGetLastError());
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, []() {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        (void)cudaGetLastError();
+    });
+    if (!fn) throw Error(AQUA_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    return fn;
+}
+
+void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n, float* out, uint32_t* err) {
+    if (n <= 0) return;
+    if (((uintptr_t)X & 15) != 0) throw Error(AQUA_ERR_INVALID_ARG, "x must be 16-byte aligned");
+    CUtensorMap map;
+    const cuuint64_t dims[2] = {64, (cuuint64_t)n};
+    const cuuint64_t strides[1] = {128};  // bytes per row
+    const cuuint32_t box[2] = {8, (cuuint32_t)kTcRows};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<uint16_t*>(X), dims,
+                                      strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw Error(AQUA_ERR_CUDA, "cuTensorMapEncodeTiled failed for the query rows");
+    AQ_CUDA(cudaFuncSetAttribute(k_nrc_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
+    const int tiles = (n + kTcRows - 1) / kTcRows;
+    const int grid = std::max(1, std::min((tiles + kTcGroups - 1) / kTcGroups, ctx->num_sms));
+    k_nrc_forward_tc<<<grid, kTcThreads, kTcSmemBytes, ctx->stream>>>(map, n, reinterpret_cast<const uint4*>(img),
+                                                                       out, err);
+    AQ_CUDA(cudaGetLastError());
+}
+
+}  // namespace aq

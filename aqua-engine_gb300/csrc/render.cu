@@ -1035,6 +1035,7 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     unsigned long long hs[16];
     AQ_CUDA(cudaMemcpyAsync(hs, w.stats, 8 * 16, cudaMemcpyDeviceToHost, st));
     AQ_CUDA(cudaStreamSynchronize(st));
+    nrc_check_tc(ctx, net);
     if (stats) {
         memset(stats, 0, sizeof(*stats));
         float ms = 0.0f, q_ms = 0.0f, t_ms = 0.0f;

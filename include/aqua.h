@@ -337,7 +337,14 @@ typedef struct aqua_nrc_cfg {
     float ema_decay;              /* > 0: inference (aqua_nrc_forward and the
                                      cached renderer) uses an exponential
                                      moving average of the trained weights  */
+    int32_t forward_kernel;       /* inference kernel, AQUA_NRC_KERNEL_*    */
 } aqua_nrc_cfg;
+
+/* Inference kernels: AUTO picks TCGEN05 (5th-generation tensor cores, the
+ * accumulator in tensor memory); MMA_SYNC is the warp-level tensor-core
+ * kernel the training step also uses. Both give the same results up to the
+ * order of FP32 accumulation. */
+enum { AQUA_NRC_KERNEL_AUTO = 0, AQUA_NRC_KERNEL_MMA_SYNC = 1, AQUA_NRC_KERNEL_TCGEN05 = 2 };
 
 AQUA_API void aqua_nrc_defaults(aqua_nrc_cfg* cfg);
 AQUA_API aqua_status aqua_nrc_create(aqua_ctx* ctx, const aqua_nrc_cfg* cfg, aqua_nrc** out);

@@ -56,17 +56,54 @@ def test_encode_matches_oracle(net):
     assert np.abs(got - ref).mean() < 2e-3
 
 
-def test_forward_matches_oracle(net):
+@pytest.mark.parametrize("kernel", ["mma_sync", "tcgen05"])
+@pytest.mark.parametrize("rows", [1, 127, 4099])
+def test_forward_matches_oracle(gpu_ctx, kernel, rows):
+    """Both inference kernels against the bf16-emulating FP64 oracle; 4099
+    rows is ragged for both the 16-row (mma.sync) and 128-row (tcgen05)
+    tiles, 1 and 127 leave most of a single tcgen05 tile empty."""
+    import aqua
     import pyoracle
 
-    raw = rand_raw(4099, 2)  # not a multiple of 16: exercises the ragged tile
-    x = net.encode(raw)
-    w = net.weights()
-    y = net.forward(x)
+    k = aqua.NRC_KERNEL_MMA_SYNC if kernel == "mma_sync" else aqua.NRC_KERNEL_TCGEN05
+    net = aqua.Nrc(gpu_ctx, seed=3, bbox_min=[-1, -1, -1], bbox_max=[1, 1, 1], forward_kernel=k)
+    try:
+        raw = rand_raw(rows, 2)
+        x = net.encode(raw)
+        w = net.weights()
+        y = net.forward(x)
+    finally:
+        net.free()
     ref = pyoracle.mlp_forward(w, pyoracle.bf16_to_float(x), emulate_bf16=True)
     scale = np.abs(ref).max()
     assert np.abs(y - ref).max() <= 1e-2 * scale
     assert np.abs(y - ref).mean() <= 1e-3 * scale
+
+
+def test_tcgen05_matches_mma_sync(gpu_ctx):
+    """The two inference kernels on the same weights and 300K rows (many
+    tiles per CTA): they differ only in FP32 accumulation order and the bf16
+    rounding flips it causes, so outputs agree to the forward tolerance."""
+    import aqua
+
+    nets = [aqua.Nrc(gpu_ctx, seed=11, bbox_min=[-1, -1, -1], bbox_max=[1, 1, 1], forward_kernel=k)
+            for k in (aqua.NRC_KERNEL_MMA_SYNC, aqua.NRC_KERNEL_TCGEN05)]
+    try:
+        rng = np.random.default_rng(12)
+        w = (rng.uniform(-0.3, 0.3, aqua.NRC_PARAMS)).astype(np.float32)
+        for n in nets:
+            n.set_weights(w)
+        raw = rand_raw(300_007, 13)
+        x = nets[0].encode(raw)
+        y0, y1 = (n.forward(x) for n in nets)
+    finally:
+        for n in nets:
+            n.free()
+    scale = np.abs(y0).max()
+    d = np.abs(y0 - y1)
+    assert d.max() <= 1e-2 * scale, d.max() / scale
+    assert d.mean() <= 1e-3 * scale
+    assert np.all(np.isfinite(y1))
 
 
 def test_gradient_matches_oracle(net):
