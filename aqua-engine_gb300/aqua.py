@@ -162,6 +162,7 @@ SIGNATURES = [
     ("aqua_nrc_get_gradients", C.c_int, [_P, _P, _P]),
     ("aqua_nrc_encode", C.c_int, [_P, _P, _P, C.c_size_t, _P, C.c_uint32]),
     ("aqua_nrc_forward", C.c_int, [_P, _P, _P, C.c_size_t, _P, C.c_uint32]),
+    ("aqua_nrc_last_ms", C.c_int, [_P, _P, C.POINTER(C.c_float)]),
     ("aqua_nrc_train_step", C.c_int, [_P, _P, _P, _P, C.c_size_t, C.POINTER(C.c_double), C.c_uint32]),
     ("aqua_render_nrc", C.c_int, [_P, _P, C.POINTER(IntegratorCfg), C.POINTER(Tuning), _P, _P, C.c_uint32,
                                   C.POINTER(Stats)]),
@@ -221,6 +222,19 @@ class Nrc:
         self.ctx._check(self.ctx.lib.aqua_nrc_encode(self.ctx.handle, self.handle, _ptr(raw), raw.shape[0],
                                                      _ptr(x), 0))
         return x
+
+    def forward_device(self, x_ptr: int, n: int, out_ptr: int) -> float:
+        """Inference on device buffers (x: n x 64 bf16, out: n x 3 fp32);
+        returns the kernel's device milliseconds (CUDA events)."""
+        self.ctx._check(self.ctx.lib.aqua_nrc_forward(self.ctx.handle, self.handle, C.c_void_p(x_ptr), n,
+                                                      C.c_void_p(out_ptr), 3))
+        ms = C.c_float()
+        self.ctx._check(self.ctx.lib.aqua_nrc_last_ms(self.ctx.handle, self.handle, C.byref(ms)))
+        return ms.value
+
+    def encode_device(self, raw_ptr: int, n: int, x_ptr: int):
+        self.ctx._check(self.ctx.lib.aqua_nrc_encode(self.ctx.handle, self.handle, C.c_void_p(raw_ptr), n,
+                                                     C.c_void_p(x_ptr), 1))
 
     def forward(self, x_bf16: np.ndarray) -> np.ndarray:
         x = np.ascontiguousarray(x_bf16, np.uint16).reshape(-1, 64)

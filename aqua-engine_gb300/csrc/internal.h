@@ -151,6 +151,7 @@ struct aqua_scene {
 struct aqua_nrc {
     aq::NrcNet net;
     aq::DevBuf stage_in, stage_tgt, stage_out;  // staging for host-pointer calls
+    float last_ms = 0.0f;                        // device time of the last AQUA_NRC_TIMING call
 };
 
 struct aqua_ctx {

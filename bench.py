@@ -326,6 +326,56 @@ def run_interior_metric(ctx, warmup: int = 1, steps: int = 2):
             "ms_per_step": ms / steps, "steps": steps, "warmup": warmup}
 
 
+NRC_INFER_WORKLOAD = {"workload": "nrc-inference-16777216-rows", "rows": 1 << 24,
+                      "network": "64 -> 5 x 64 (ReLU) -> 3, bf16 operands, fp32 accumulation",
+                      "inputs": "encoded from uniform random vertex features (positions in the unit box, "
+                                "unit directions and normals, albedos), seed 21"}
+NRC_FLOP_PER_ROW = 2 * (5 * 64 * 64 + 3 * 64)  # 41,344 useful multiply-adds x 2
+NRC_BYTES_PER_ROW = 128 + 12                   # bf16 input row + fp32 output
+
+
+def run_nrc_inference_metric(ctx, bf16_peak: float, peak_src: str, warmup: int = 3, steps: int = 10,
+                             rows: int = NRC_INFER_WORKLOAD["rows"]):
+    """The cache's inference kernels alone on 16.8M encoded rows (2.1 GB of
+    input, > L2): rows/s and the tensor roofline of the tcgen05 kernel, with
+    the mma.sync kernel beside it. Device time from CUDA events on the
+    library's stream."""
+    import torch
+    import aqua
+
+    W = dict(NRC_INFER_WORKLOAD)
+    n = W["rows"] = rows
+    W["workload"] = f"nrc-inference-{rows}-rows"
+    g = torch.Generator(device="cuda").manual_seed(21)
+    raw = torch.rand((n, 16), generator=g, device="cuda", dtype=torch.float32)
+    for sl in (slice(3, 6), slice(6, 9)):
+        v = raw[:, sl] * 2 - 1
+        raw[:, sl] = v / v.norm(dim=1, keepdim=True).clamp_min(1e-6)
+    x = torch.empty((n, 64), dtype=torch.int16, device="cuda")
+    out = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    res = {}
+    for name, kern in (("tcgen05", aqua.NRC_KERNEL_TCGEN05), ("mma_sync", aqua.NRC_KERNEL_MMA_SYNC)):
+        net = aqua.Nrc(ctx, seed=3, bbox_min=[0, 0, 0], bbox_max=[1, 1, 1], forward_kernel=kern)
+        net.encode_device(raw.data_ptr(), n, x.data_ptr())
+        for _ in range(warmup):
+            net.forward_device(x.data_ptr(), n, out.data_ptr())
+        ms = [net.forward_device(x.data_ptr(), n, out.data_ptr()) for _ in range(steps)]
+        net.free()
+        t = sum(ms) / len(ms) * 1e-3
+        res[name] = {"rows_per_s": n / t, "ms_per_launch": t * 1e3, "tflops": n * NRC_FLOP_PER_ROW / t / 1e12,
+                     "gbs": n * NRC_BYTES_PER_ROW / t / 1e9}
+    del raw, x, out
+    tc = res["tcgen05"]
+    return {"config": W, "unit": "Grows/s", "value": tc["rows_per_s"] / 1e9,
+            "mma_sync_value": res["mma_sync"]["rows_per_s"] / 1e9, "steps": steps, "warmup": warmup,
+            "kernels": res,
+            "roofline": {"bound": "tensor", "achieved": tc["tflops"], "peak": bf16_peak, "unit": "TFLOP/s",
+                         "frac": tc["tflops"] / bf16_peak, "peak_source": peak_src,
+                         "kernel": "k_nrc_forward_tc (tcgen05 MLP inference)",
+                         "flop_per_row": NRC_FLOP_PER_ROW, "hbm_bytes_per_row": NRC_BYTES_PER_ROW,
+                         "hbm_gbs": tc["gbs"]}}
+
+
 BATCH_WORKLOAD = {"workload": "batch-64-jobs-4-scenes",
                   "scenes": ["Cornell Lambert (36 tris)", "Cornell GGX (36 tris)",
                              "synthetic interior (1.15M tris, 8 textures)", "random-sphere field (4.0M tris)"],
@@ -482,11 +532,16 @@ def run_gpu(args, world, rank, local, pg):
     roofline["frac_of_l2_copy"] = achieved / l2["gbs"]
     interior = run_interior_metric(ctx) if rank == 0 and not args.no_interior else None
     nrc = None
-    if rank == 0 and not args.no_nrc:
+    if rank == 0 and not args.no_nrc and not args.no_nrc_time:
         nrc = run_nrc_metric(ctx, args.nrc_budget)
     batch = None
     if rank == 0 and not args.no_batch:
         batch = run_batch_metric(ctx)
+    nrc_inf = None
+    if rank == 0 and not args.no_nrc:
+        bf16_peak = peaks.get("bf16_tflops", 1900.0)
+        nrc_inf = run_nrc_inference_metric(ctx, bf16_peak, "measured (burst)" if "bf16_tflops" in peaks else "fallback",
+                                           rows=args.nrc_rows)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -511,6 +566,7 @@ def run_gpu(args, world, rank, local, pg):
                 "gpu_launches": gpu_launches,
                 "interior": interior,
                 "nrc_time_to_relmse": nrc,
+                "nrc_inference": nrc_inf,
                 "batch": batch,
                 "stage_ms_per_step": {"trace": trace_ms / args.steps,
                                       "shade": sum(s.shade_ms for s in steps) / args.steps,
@@ -526,9 +582,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="aqua", choices=["aqua", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--cpu-seconds", type=float, default=13.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-nrc", action="store_true", help="skip the cached-vs-plain time-to-relMSE measurement")
+    ap.add_argument("--no-nrc", action="store_true", help="skip both radiance-cache measurements")
+    ap.add_argument("--no-nrc-time", action="store_true", help="skip the cached-vs-plain time-to-relMSE measurement")
+    ap.add_argument("--nrc-rows", type=int, default=NRC_INFER_WORKLOAD["rows"],
+                    help="rows of the cache-inference measurement (smaller only for profiling captures)")
     ap.add_argument("--nrc-budget", type=float, default=60.0, help="seconds per arm of that measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-job batched-serving measurement")
     ap.add_argument("--no-interior", action="store_true", help="skip the 1080p interior measurement")

@@ -327,7 +327,12 @@ AQUA_API uint64_t aqua_workspace_bytes(const aqua_ctx* ctx);
 typedef struct aqua_nrc aqua_nrc;
 
 enum { AQUA_NRC_PARAMS = 20672, AQUA_NRC_INPUTS = 64, AQUA_NRC_RAW = 16 };
-enum { AQUA_NRC_DEVICE_PTRS = 1u << 0 };
+enum {
+    AQUA_NRC_DEVICE_PTRS = 1u << 0, /* x / raw / out / target are device pointers */
+    AQUA_NRC_TIMING = 1u << 1       /* time the call's device work with CUDA events
+                                       on the context's stream; read it with
+                                       aqua_nrc_last_ms                          */
+};
 
 typedef struct aqua_nrc_cfg {
     float learning_rate;          /* Adam step size                         */
@@ -361,6 +366,8 @@ AQUA_API aqua_status aqua_nrc_encode(aqua_ctx* ctx, aqua_nrc* nrc, const float* 
 /* out: n x 3 floats (radiance). */
 AQUA_API aqua_status aqua_nrc_forward(aqua_ctx* ctx, aqua_nrc* nrc, const uint16_t* x, size_t n, float* out,
                                       uint32_t flags);
+/* Device milliseconds of the last call made with AQUA_NRC_TIMING. */
+AQUA_API aqua_status aqua_nrc_last_ms(aqua_ctx* ctx, aqua_nrc* nrc, float* ms);
 /* One Adam step on a batch of n records (x, target radiance n x 3); loss =
  * the batch's mean relative L2 loss before the step (may be NULL). */
 AQUA_API aqua_status aqua_nrc_train_step(aqua_ctx* ctx, aqua_nrc* nrc, const uint16_t* x, const float* target,
