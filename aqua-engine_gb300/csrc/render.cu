@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(128) k_trace_ext(DevScene S, WaveParams P, Wav
 // so far) so that the radiance leaving each of their vertices becomes a
 // training target once the path is complete.
 template <bool SORTED, bool NRC = false>
-__global__ void __launch_bounds__(128, 8) k_shade(DevScene S, WaveParams P, WavePtrs W, uint32_t cnt_in,
+__global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, WavePtrs W, uint32_t cnt_in,
                                                uint32_t cnt_out) {
     __shared__ float lut[256];
     __shared__ uint32_t prefix[257];
