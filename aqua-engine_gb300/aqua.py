@@ -163,6 +163,7 @@ SIGNATURES = [
     ("aqua_nrc_encode", C.c_int, [_P, _P, _P, C.c_size_t, _P, C.c_uint32]),
     ("aqua_nrc_forward", C.c_int, [_P, _P, _P, C.c_size_t, _P, C.c_uint32]),
     ("aqua_nrc_last_ms", C.c_int, [_P, _P, C.POINTER(C.c_float)]),
+    ("aqua_decode_jpeg", C.c_int, [_P, _P, C.c_size_t, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P]),
     ("aqua_nrc_train_step", C.c_int, [_P, _P, _P, _P, C.c_size_t, C.POINTER(C.c_double), C.c_uint32]),
     ("aqua_render_nrc", C.c_int, [_P, _P, C.POINTER(IntegratorCfg), C.POINTER(Tuning), _P, _P, C.c_uint32,
                                   C.POINTER(Stats)]),
@@ -468,6 +469,15 @@ class Context:
         t = Tuning()
         self._check(self.lib.aqua_autotune_batch(self.handle, arr, len(jobs), C.byref(t)))
         return t
+
+    def decode_jpeg(self, data: bytes) -> np.ndarray:
+        """JPEG bytes -> (h, w, 3) uint8 RGB, row 0 at the top."""
+        buf = np.frombuffer(data, np.uint8)
+        w, h = C.c_int32(), C.c_int32()
+        self._check(self.lib.aqua_decode_jpeg(self.handle, _ptr(buf), buf.size, C.byref(w), C.byref(h), None))
+        out = np.zeros((h.value, w.value, 3), np.uint8)
+        self._check(self.lib.aqua_decode_jpeg(self.handle, _ptr(buf), buf.size, C.byref(w), C.byref(h), _ptr(out)))
+        return out
 
     def workspace_bytes(self) -> int:
         return int(self.lib.aqua_workspace_bytes(self.handle))

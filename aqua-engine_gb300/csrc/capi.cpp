@@ -8,6 +8,7 @@
 #include <new>
 
 #include "internal.h"
+#include "jpeg.h"
 #include "nrc.h"
 
 namespace {
@@ -417,6 +418,19 @@ AQUA_API aqua_status aqua_scene_export_texture(aqua_ctx* ctx, const aqua_scene* 
         if (w) *w = t.w;
         if (h) *h = t.h;
         if (rgba) memcpy(rgba, t.rgba.data(), t.rgba.size());
+    });
+}
+
+AQUA_API aqua_status aqua_decode_jpeg(aqua_ctx* ctx, const uint8_t* data, size_t n, int32_t* w, int32_t* h,
+                                      uint8_t* rgb) {
+    return guard(ctx, [&]() {
+        need(data != nullptr || n == 0, "data is NULL");
+        JpegImage img;
+        std::string err = jpeg_decode(data, n, img);
+        if (!err.empty()) throw Error(AQUA_ERR_UNSUPPORTED, "JPEG: " + err);
+        if (w) *w = img.w;
+        if (h) *h = img.h;
+        if (rgb) memcpy(rgb, img.rgb.data(), img.rgb.size());
     });
 }
 

@@ -6,10 +6,13 @@
 #include <cmath>
 #include <cstring>
 #include <fstream>
+#include <iterator>
+#include <map>
 #include <sstream>
 #include <thread>
 
 #include "aq_math.h"
+#include "jpeg.h"
 #include "json.h"
 
 namespace aq {
@@ -295,7 +298,52 @@ struct Bsdf_ {
     v3 emission;
 };
 
-Bsdf_ read_bsdf(const Json& j, const std::string& dir, bool allow_missing, const std::string& name) {
+// Decoded `Image` textures by file, so materials that share a file share a
+// texture. Texture rows are stored bottom-up (row 0 = the image's last row):
+// v = 0 is the bottom edge of the image, as in the OBJ texture coordinates
+// the .mesh files carry.
+struct TexCache {
+    HostScene& s;
+    std::map<std::string, int> index;
+};
+
+// Index of the decoded texture, or -1 when it is missing or undecodable and
+// allow_missing is set (the caller then uses mid-grey).
+int image_texture(TexCache& tc, const std::string& full, bool allow_missing, const std::string& name) {
+    auto it = tc.index.find(full);
+    if (it != tc.index.end()) return it->second;
+    std::ifstream f(full, std::ios::binary);
+    if (!f) {
+        if (allow_missing) return tc.index[full] = -1;
+        throw SceneError(AQUA_ERR_MISSING_ASSET, "bsdf \"" + name + "\": texture " + full + " is missing");
+    }
+    std::vector<uint8_t> data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    JpegImage img;
+    std::string err = jpeg_decode(data.data(), data.size(), img);
+    if (!err.empty()) {
+        if (allow_missing) return tc.index[full] = -1;
+        throw SceneError(AQUA_ERR_UNSUPPORTED, "bsdf \"" + name + "\": texture " + full + ": " + err);
+    }
+    Texture t;
+    t.w = img.w;
+    t.h = img.h;
+    t.rgba.resize((size_t)img.w * (size_t)img.h * 4);
+    for (int y = 0; y < img.h; ++y) {
+        const uint8_t* src = &img.rgb[(size_t)(img.h - 1 - y) * (size_t)img.w * 3];
+        uint8_t* dst = &t.rgba[(size_t)y * (size_t)img.w * 4];
+        for (int x = 0; x < img.w; ++x) {
+            dst[4 * x] = src[3 * x];
+            dst[4 * x + 1] = src[3 * x + 1];
+            dst[4 * x + 2] = src[3 * x + 2];
+            dst[4 * x + 3] = 255;
+        }
+    }
+    tc.s.textures.push_back(std::move(t));
+    return tc.index[full] = (int)tc.s.textures.size() - 1;
+}
+
+Bsdf_ read_bsdf(const Json& j, const std::string& dir, bool allow_missing, const std::string& name,
+                TexCache& tc) {
     if (!j.is_object() || j.obj.size() != 1) throw JsonError("bsdf must be a one-key object");
     if (j.obj[0].first != "Principled")
         throw SceneError(AQUA_ERR_UNSUPPORTED, "bsdf \"" + name + "\": variant \"" + j.obj[0].first +
@@ -317,15 +365,13 @@ Bsdf_ read_bsdf(const Json& j, const std::string& dir, bool allow_missing, const
     if (col) {
         TexVal t = read_tex(*col);
         if (t.image) {
-            std::string full = dir + "/" + t.path;
-            std::ifstream f(full, std::ios::binary);
-            if (!f && !allow_missing)
-                throw SceneError(AQUA_ERR_MISSING_ASSET, "bsdf \"" + name + "\": texture " + full + " is missing");
-            if (!allow_missing)
-                throw SceneError(AQUA_ERR_UNSUPPORTED,
-                                 "bsdf \"" + name + "\": JPEG texture " + full +
-                                     " needs a decoder this build does not ship");
-            base = mk(0.5f, 0.5f, 0.5f);  // mid-grey stand-in
+            int ti = image_texture(tc, dir + "/" + t.path, allow_missing, name);
+            if (ti >= 0) {
+                base = mk(1.0f, 1.0f, 1.0f);  // the texture is the base colour
+                b.m.base_texture = ti;
+            } else {
+                base = mk(0.5f, 0.5f, 0.5f);  // mid-grey stand-in
+            }
         } else {
             base = t.value;
         }
@@ -361,6 +407,7 @@ HostScene load_scene_json(const std::string& path, bool allow_missing) {
     size_t slash = path.find_last_of('/');
     if (slash != std::string::npos) dir = path.substr(0, slash);
     HostScene s;
+    TexCache tc{s, {}};
     std::vector<v3> mat_emission;
     try {
         Json root = json_parse(text);
@@ -369,7 +416,7 @@ HostScene load_scene_json(const std::string& path, bool allow_missing) {
         std::vector<std::string> names;
         if (const Json* nb = root.find("named_bsdfs")) {
             for (auto& kv : nb->obj) {
-                Bsdf_ b = read_bsdf(kv.second, dir, allow_missing, kv.first);
+                Bsdf_ b = read_bsdf(kv.second, dir, allow_missing, kv.first, tc);
                 s.mats.push_back(b.m);
                 s.mat_names.push_back(kv.first);
                 mat_emission.push_back(b.emission);
@@ -426,7 +473,7 @@ HostScene load_scene_json(const std::string& path, bool allow_missing) {
                     if (s.mat_names[i] == nm) mat = (int)i;
                 if (mat < 0) throw JsonError("shape refers to unknown bsdf \"" + nm + "\"");
             } else {
-                Bsdf_ b = read_bsdf(bref, dir, allow_missing, file);
+                Bsdf_ b = read_bsdf(bref, dir, allow_missing, file, tc);
                 s.mats.push_back(b.m);
                 s.mat_names.push_back(file);
                 mat_emission.push_back(b.emission);

@@ -227,9 +227,12 @@ AQUA_API int aqua_version(void);
  * lights, shapes) with its BSON meshes from the JSON's directory. A missing
  * mesh (e.g. living_room_Default_43.mesh, .MISSING_LARGE_BLOBS:1) fails with
  * AQUA_ERR_MISSING_ASSET unless allow_missing is set, which skips it. Image
- * textures (room.json:6) need a JPEG decoder this build does not ship: they
- * fail with AQUA_ERR_UNSUPPORTED unless allow_missing is set, which replaces
- * them by the material's mid-grey. */
+ * textures (room.json:6) are decoded by the built-in JPEG decoder (Huffman
+ * sequential and progressive, 8-bit, grey or YCbCr); a file it refuses
+ * (arithmetic coding, 12-bit, lossless) fails with AQUA_ERR_UNSUPPORTED and a
+ * missing file with AQUA_ERR_MISSING_ASSET, unless allow_missing is set, which
+ * replaces the texture by mid-grey. Texture rows are stored bottom-up, so
+ * v = 0 is the bottom edge of the image (OBJ texture coordinates). */
 AQUA_API aqua_status aqua_load_scene_json(aqua_ctx* ctx, const char* path,
                                           int32_t allow_missing, aqua_scene** out);
 /* Procedural scenes 1..5: 1 = Cornell box (Lambert), 2 = Cornell box with GGX
@@ -262,10 +265,16 @@ AQUA_API aqua_status aqua_scene_export_materials(aqua_ctx* ctx, const aqua_scene
                                                  aqua_material* out);
 AQUA_API aqua_status aqua_scene_export_lights(aqua_ctx* ctx, const aqua_scene* scene,
                                               aqua_light* out);
-/* Texture i as RGBA8, row-major, sRGB-encoded. Pass rgba = NULL to query the size. */
+/* Texture i as RGBA8, row-major from v = 0, sRGB-encoded. Pass rgba = NULL to query the size. */
 AQUA_API aqua_status aqua_scene_export_texture(aqua_ctx* ctx, const aqua_scene* scene,
                                                int32_t i, int32_t* width, int32_t* height,
                                                uint8_t* rgba);
+/* Decodes JPEG bytes (the decoder `Image` textures go through; it stands in
+ * for the reference's `image` crate, Cargo.toml:13) into 8-bit RGB, row 0 =
+ * the top of the image. Pass rgb = NULL to query the size. Works on a
+ * host-only context. */
+AQUA_API aqua_status aqua_decode_jpeg(aqua_ctx* ctx, const uint8_t* data, size_t n, int32_t* width,
+                                      int32_t* height, uint8_t* rgb);
 /* The flattened BVH as the device holds it: nodes = 16 floats per node (four
  * 16-byte words, layout in bvh.h), tri_order[k] = scene index of the k-th
  * triangle in leaf order. */

@@ -223,6 +223,28 @@ def test_reference_room(host_ctx):
     assert i.num_triangles == f["triangles_present"] == 394269
     assert i.num_meshes == f["meshes_present"] == 152
     assert [i.width, i.height] == f["res"]
+    # Every `Image` texture is decoded (JPEG), once per file.
+    room = json.load(open(os.path.join(REF_SCENES, "room.json")))
+    images = set()
+
+    def walk(x):
+        if isinstance(x, dict):
+            for k, v in x.items():
+                if k == "Image":
+                    images.add(v.replace("\\", "/"))
+                walk(v)
+        elif isinstance(x, list):
+            for v in x:
+                walk(v)
+
+    walk(room)
+    assert len(images) >= 10 and i.num_textures == len(images)
+    textured = [m for m in s.materials() if m.base_texture >= 0]
+    assert textured and all(list(m.base_color) == [1.0, 1.0, 1.0] for m in textured)
+    facts = json.load(open(os.path.join(GOLDEN, "jpeg_facts.json")))["files"]
+    sizes = sorted(s.texture(k).shape[:2] for k in range(i.num_textures))
+    expect = sorted((facts[os.path.basename(p)]["height"], facts[os.path.basename(p)]["width"]) for p in images)
+    assert sizes == expect
     s.free()
 
 
