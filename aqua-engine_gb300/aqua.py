@@ -164,6 +164,9 @@ SIGNATURES = [
     ("aqua_nrc_forward", C.c_int, [_P, _P, _P, C.c_size_t, _P, C.c_uint32]),
     ("aqua_nrc_last_ms", C.c_int, [_P, _P, C.POINTER(C.c_float)]),
     ("aqua_decode_jpeg", C.c_int, [_P, _P, C.c_size_t, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P]),
+    ("aqua_convert_obj", C.c_int, [_P, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32,
+                                   C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    ("aqua_write_image", C.c_int, [_P, C.c_char_p, _P, C.c_int32, C.c_int32]),
     ("aqua_nrc_train_step", C.c_int, [_P, _P, _P, _P, C.c_size_t, C.POINTER(C.c_double), C.c_uint32]),
     ("aqua_render_nrc", C.c_int, [_P, _P, C.POINTER(IntegratorCfg), C.POINTER(Tuning), _P, _P, C.c_uint32,
                                   C.POINTER(Stats)]),
@@ -478,6 +481,19 @@ class Context:
         out = np.zeros((h.value, w.value, 3), np.uint8)
         self._check(self.lib.aqua_decode_jpeg(self.handle, _ptr(buf), buf.size, C.byref(w), C.byref(h), _ptr(out)))
         return out
+
+    def convert_obj(self, obj_path: str, out_dir: str, scene_name: str = "scene.json", width: int = 512,
+                    height: int = 512):
+        """OBJ + MTL -> BSON meshes + scene JSON in out_dir; returns (meshes, triangles)."""
+        m, t = C.c_int32(), C.c_int32()
+        self._check(self.lib.aqua_convert_obj(self.handle, obj_path.encode(), out_dir.encode(), scene_name.encode(),
+                                              width, height, C.byref(m), C.byref(t)))
+        return m.value, t.value
+
+    def write_image(self, path: str, rgb: np.ndarray, width: int, height: int):
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        assert rgb.size == width * height * 3
+        self._check(self.lib.aqua_write_image(self.handle, path.encode(), _ptr(rgb), width, height))
 
     def workspace_bytes(self) -> int:
         return int(self.lib.aqua_workspace_bytes(self.handle))

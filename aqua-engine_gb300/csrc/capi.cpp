@@ -9,6 +9,7 @@
 
 #include "internal.h"
 #include "jpeg.h"
+#include "obj.h"
 #include "nrc.h"
 
 namespace {
@@ -431,6 +432,27 @@ AQUA_API aqua_status aqua_decode_jpeg(aqua_ctx* ctx, const uint8_t* data, size_t
         if (w) *w = img.w;
         if (h) *h = img.h;
         if (rgb) memcpy(rgb, img.rgb.data(), img.rgb.size());
+    });
+}
+
+AQUA_API aqua_status aqua_convert_obj(aqua_ctx* ctx, const char* obj_path, const char* out_dir,
+                                      const char* scene_name, int32_t width, int32_t height, int32_t* meshes,
+                                      int32_t* triangles) {
+    return guard(ctx, [&]() {
+        need(obj_path && out_dir && scene_name, "obj_path, out_dir and scene_name must be non-NULL");
+        need(width > 0 && height > 0, "width and height must be positive");
+        ObjConvertResult r = convert_obj(obj_path, out_dir, scene_name, width, height);
+        if (meshes) *meshes = r.meshes;
+        if (triangles) *triangles = r.triangles;
+    });
+}
+
+AQUA_API aqua_status aqua_write_image(aqua_ctx* ctx, const char* path, const float* rgb, int32_t width,
+                                      int32_t height) {
+    return guard(ctx, [&]() {
+        need(path && rgb, "path and rgb must be non-NULL");
+        need(width > 0 && height > 0, "width and height must be positive");
+        write_image(path, rgb, width, height);
     });
 }
 

@@ -365,7 +365,7 @@ Bsdf_ read_bsdf(const Json& j, const std::string& dir, bool allow_missing, const
     if (col) {
         TexVal t = read_tex(*col);
         if (t.image) {
-            int ti = image_texture(tc, dir + "/" + t.path, allow_missing, name);
+            int ti = image_texture(tc, t.path[0] == '/' ? t.path : dir + "/" + t.path, allow_missing, name);
             if (ti >= 0) {
                 base = mk(1.0f, 1.0f, 1.0f);  // the texture is the base colour
                 b.m.base_texture = ti;

@@ -275,6 +275,23 @@ AQUA_API aqua_status aqua_scene_export_texture(aqua_ctx* ctx, const aqua_scene* 
  * host-only context. */
 AQUA_API aqua_status aqua_decode_jpeg(aqua_ctx* ctx, const uint8_t* data, size_t n, int32_t* width,
                                       int32_t* height, uint8_t* rgb);
+/* Converts a Wavefront OBJ and the MTL libraries it names into the scene
+ * format aqua_load_scene_json reads, as the reference's tobj-based
+ * conversion (Cargo.toml:23) produced scenes/CornellBox-Original_*.mesh and
+ * scenes/cbox.json: one BSON .mesh per OBJ group, `<obj stem>_<group>_<k>.mesh`
+ * (name, vertices, normals, texcoords, indices; faces fanned into
+ * triangles), and out_dir/scene_name with the MTL materials (Kd as an Srgb
+ * colour, Ke as emission, map_Kd as an Image texture; metallic 0, specular
+ * 0, roughness 0.4), a camera of width x height framing the model, and the
+ * shapes. meshes / triangles may be NULL. Works on a host-only context. */
+AQUA_API aqua_status aqua_convert_obj(aqua_ctx* ctx, const char* obj_path, const char* out_dir,
+                                      const char* scene_name, int32_t width, int32_t height,
+                                      int32_t* meshes, int32_t* triangles);
+/* Writes a W x H x 3 float film (row 0 at the top) to `path`: ".pfm" as
+ * little-endian float PFM, ".ppm" as 8-bit P6 of the sRGB-encoded film
+ * clamped to [0, 1]. */
+AQUA_API aqua_status aqua_write_image(aqua_ctx* ctx, const char* path, const float* rgb, int32_t width,
+                                      int32_t height);
 /* The flattened BVH as the device holds it: nodes = 16 floats per node (four
  * 16-byte words, layout in bvh.h), tri_order[k] = scene index of the k-th
  * triangle in leaf order. */
