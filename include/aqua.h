@@ -104,7 +104,7 @@ typedef struct aqua_integrator_cfg {
     uint64_t seed;           /* RNG seed: PCG32 stream per pixel            */
     int32_t spp_offset;      /* first sample index (progressive rendering)  */
     int32_t nrc_train_samples; /* NRC: training records per frame          */
-    int32_t nrc_query_vertex;  /* NRC: query the cache at this vertex       */
+    int32_t nrc_query_vertex;  /* NRC: query the cache at this vertex (>= 2; default 4) */
     int32_t reserved0;
 } aqua_integrator_cfg;
 
