@@ -200,6 +200,124 @@ __device__ __forceinline__ TraceResult traverse_fast(const DevScene& S, v3 o, v3
     }
 }
 
+// Persistent traversal of a queue of n rays with ray replacement (Aila &
+// Laine 2009, sec. 4: "replacing terminated rays"): each lane holds its own
+// ray; once at least kRefillLanes lanes of the warp have finished theirs (or
+// all have), the idle lanes take the next rays from *cursor together (one
+// atomic per warp). Between refills every lane runs rounds of
+// traverse_fast: walk inner nodes with postponed leaves, then test the
+// parked leaves. Boxes, culling and triangle tests are those of traverse(),
+// so every ray's result is the one traverse_fast returns.
+//   load(i, o, d, tmin, tmax) -> uint32_t tag: fetches ray i of the queue;
+//   done(tag, r): called once per ray, by the lanes finishing in the same
+//                 round together (warp collectives inside are allowed).
+constexpr int kRefillLanes = 16;
+
+template <bool ANY, class Load, class Done>
+__device__ __forceinline__ void traverse_queue(const DevScene& S, uint32_t n, uint32_t* cursor, Load load,
+                                               Done done) {
+    const unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    RayPre rp;
+    RayShear sh;
+    TraceResult r;
+    int32_t stack[kStackSize];
+    int sp = 0;
+    int32_t node = kTraversalDone, leaf = 0;
+    uint32_t tag = 0;
+    bool have = false, drained = false;
+    while (true) {
+        const unsigned idle = __ballot_sync(kFull, !have);
+        if (!drained && idle != 0u && (__popc(idle) >= kRefillLanes || idle == kFull)) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(cursor, (uint32_t)__popc(idle));
+            base = __shfl_sync(kFull, base, leader);
+            if (base + (uint32_t)__popc(idle) >= n) drained = true;
+            if (!have) {
+                const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (i < n) {
+                    v3 o, d;
+                    float tmin, tmax;
+                    tag = load(i, o, d, tmin, tmax);
+                    rp.o = o;
+                    rp.invd = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+                    rp.tmin = tmin;
+                    rp.tmax = tmax;
+                    sh = make_shear(o, d);
+                    r.t = tmax; r.u = 0.0f; r.v = 0.0f; r.tri = -1; r.id = 0x7fffffff;
+                    sp = 0;
+                    node = 0;
+                    leaf = 0;
+                    have = true;
+                }
+            }
+        }
+        if (!__any_sync(kFull, have)) break;
+        if (!have) continue;
+        // One round of traverse_fast.
+        while (node >= 0) {
+            const float4* np = S.nodes + 4 * (size_t)node;
+            float4 w0 = ldg_(np), w1 = ldg_(np + 1), w2 = ldg_(np + 2);
+            int4 w3 = ldg_(reinterpret_cast<const int4*>(np + 3));
+            float t0 = slab_entry(w0.x, w0.y, w0.z, w0.w, w2.x, w2.y, rp, r.t);
+            float t1 = slab_entry(w1.x, w1.y, w1.z, w1.w, w2.z, w2.w, rp, r.t);
+            bool h0 = t0 != INFINITY, h1 = t1 != INFINITY;
+            if (h0 && h1) {
+                bool swap = t1 < t0;
+                stack[sp++] = swap ? w3.x : w3.y;
+                node = swap ? w3.y : w3.x;
+            } else if (h0) {
+                node = w3.x;
+            } else if (h1) {
+                node = w3.y;
+            } else {
+                node = sp > 0 ? stack[--sp] : kTraversalDone;
+            }
+            if (node < 0 && node != kTraversalDone && leaf == 0) {
+                leaf = node;
+                node = sp > 0 ? stack[--sp] : kTraversalDone;
+            }
+            if (!__any_sync(__activemask(), leaf == 0)) break;
+        }
+        while (leaf < 0) {
+            int32_t code = ~leaf;
+            int32_t first = code >> 3, cnt = code & 7;
+            bool stop = false;
+            for (int k = 0; k < cnt; ++k) {
+                const float4* tp = S.tris + 3 * (size_t)(first + k);
+                float4 a = ldg_(tp), b = ldg_(tp + 1), c = ldg_(tp + 2);
+                TriHit h = intersect_tri(sh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), rp.tmin,
+                                         rp.tmax);
+                if (h.hit) {
+                    int32_t id = __float_as_int(a.w);
+                    if (ANY) {
+                        r.t = h.t; r.tri = first + k; r.id = id;
+                        stop = true;
+                        break;
+                    }
+                    if (h.t < r.t || (h.t == r.t && id < r.id)) {
+                        r.t = h.t; r.u = h.u; r.v = h.v; r.tri = first + k; r.id = id;
+                    }
+                }
+            }
+            leaf = 0;
+            if (stop) {
+                node = kTraversalDone;
+                break;
+            }
+            if (node < 0 && node != kTraversalDone) {
+                leaf = node;
+                node = sp > 0 ? stack[--sp] : kTraversalDone;
+            }
+        }
+        if (node == kTraversalDone) {
+            done(tag, r);
+            have = false;
+        }
+    }
+}
+
 // Warp-aggregated append: lanes with pred set get consecutive slots of *ctr.
 __device__ __forceinline__ uint32_t warp_append(uint32_t* ctr, bool pred) {
     unsigned mask = __ballot_sync(__activemask(), pred);

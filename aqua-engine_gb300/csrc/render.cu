@@ -194,19 +194,9 @@ __global__ void __launch_bounds__(128) k_trace_ext(DevScene S, WaveParams P, Wav
     }
     const int lane_id = threadIdx.x & 31;
     uint32_t nodes = 0, tris = 0;
-    // Each warp takes the next 32 rays of the queue (dynamic fetch: warps
-    // whose rays finish early take more).
-    while (true) {
-        uint32_t base = 0;
-        if (lane_id == 0) base = atomicAdd(&W.counters[kCntFetchTrace], 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const uint32_t i = base + (uint32_t)lane_id;
-        if (i >= n) continue;
-        uint32_t s = W.q_in[i];
-        float4 ro = W.ray_o[s], rd = W.ray_d[s];
-        TraceResult r = COUNT ? traverse<false, true>(S, f3(ro), f3(rd), ro.w, rd.w, nodes, tris)
-                              : traverse_fast<false>(S, f3(ro), f3(rd), ro.w, rd.w);
+    // Hit record and material bucket of slot s (lanes finishing together
+    // bin together).
+    auto finish = [&](uint32_t s, const TraceResult& r) {
         W.hit[s] = make_float4(r.t, r.u, r.v, __int_as_float(r.tri));
         if (SORTED) {
             uint32_t b = r.tri < 0 ? P.nb - 1
@@ -218,6 +208,34 @@ __global__ void __launch_bounds__(128) k_trace_ext(DevScene S, WaveParams P, Wav
             base = __shfl_sync(mask, base, leader);
             uint32_t pos = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
             W.bucket[(size_t)b * P.slots + pos] = s;
+        }
+    };
+    if (!COUNT) {
+        // Persistent lanes with ray replacement.
+        traverse_queue<false>(
+            S, n, &W.counters[kCntFetchTrace],
+            [&](uint32_t i, v3& o, v3& d, float& tmin, float& tmax) -> uint32_t {
+                uint32_t s = W.q_in[i];
+                float4 ro = W.ray_o[s], rd = W.ray_d[s];
+                o = f3(ro);
+                d = f3(rd);
+                tmin = ro.w;
+                tmax = rd.w;
+                return s;
+            },
+            finish);
+    } else {
+        // Canonical counting walk; each warp takes the next 32 rays.
+        while (true) {
+            uint32_t base = 0;
+            if (lane_id == 0) base = atomicAdd(&W.counters[kCntFetchTrace], 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= n) break;
+            const uint32_t i = base + (uint32_t)lane_id;
+            if (i >= n) continue;
+            uint32_t s = W.q_in[i];
+            float4 ro = W.ray_o[s], rd = W.ray_d[s];
+            finish(s, traverse<false, true>(S, f3(ro), f3(rd), ro.w, rd.w, nodes, tris));
         }
     }
     if (COUNT) {
@@ -462,23 +480,40 @@ __global__ void __launch_bounds__(128) k_shadow(DevScene S, WaveParams P, WavePt
     }
     const int lane_id = threadIdx.x & 31;
     uint32_t nodes = 0, tris = 0;
-    while (true) {
-        uint32_t base = 0;
-        if (lane_id == 0) base = atomicAdd(&W.counters[kCntFetchShadow], 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const uint32_t i = base + (uint32_t)lane_id;
-        if (i >= n) continue;
-        float4 o = W.sh_o[i], d = W.sh_d[i];
-        TraceResult r = COUNT ? traverse<true, true>(S, f3(o), f3(d), 0.0f, d.w, nodes, tris)
-                              : traverse_fast<true>(S, f3(o), f3(d), 0.0f, d.w);
+    // Unoccluded shadow ray i adds its contribution to the slot's film entry.
+    auto finish = [&](uint32_t i, const TraceResult& r) {
         if (r.tri < 0) {
             float4 c = W.sh_c[i];
-            if (!(NRC && P.visualize)) film_add(W.film, (uint32_t)__float_as_int(o.w), mk(c.x, c.y, c.z));
+            uint32_t pixel = (uint32_t)__float_as_int(W.sh_o[i].w);
+            if (!(NRC && P.visualize)) film_add(W.film, pixel, mk(c.x, c.y, c.z));
             if (NRC) {
                 int id = __float_as_int(c.w);
                 if (id > 0) ltrain_add(W.ltrain, (uint32_t)(id - 1), mk(c.x, c.y, c.z));
             }
+        }
+    };
+    if (!COUNT) {
+        traverse_queue<true>(
+            S, n, &W.counters[kCntFetchShadow],
+            [&](uint32_t i, v3& o, v3& d, float& tmin, float& tmax) -> uint32_t {
+                float4 ro = W.sh_o[i], rd = W.sh_d[i];
+                o = f3(ro);
+                d = f3(rd);
+                tmin = 0.0f;
+                tmax = rd.w;
+                return i;
+            },
+            finish);
+    } else {
+        while (true) {
+            uint32_t base = 0;
+            if (lane_id == 0) base = atomicAdd(&W.counters[kCntFetchShadow], 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= n) break;
+            const uint32_t i = base + (uint32_t)lane_id;
+            if (i >= n) continue;
+            float4 o = W.sh_o[i], d = W.sh_d[i];
+            finish(i, traverse<true, true>(S, f3(o), f3(d), 0.0f, d.w, nodes, tris));
         }
     }
     if (COUNT) {

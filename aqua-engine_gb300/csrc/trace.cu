@@ -12,15 +12,33 @@ template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_user(DevScene S, const float4* __restrict__ rays, size_t n,
                                                     float4* __restrict__ hits, unsigned long long* stats) {
     uint32_t nodes = 0, tris = 0;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        float4 a = ldg_(rays + 2 * i), b = ldg_(rays + 2 * i + 1);
-        TraceResult r = COUNT ? traverse<ANY, true>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, nodes, tris)
-                              : traverse_fast<ANY>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w);
+    auto store = [&](size_t i, const TraceResult& r) {
         float4 h;
         if (ANY) h = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(r.tri >= 0 ? 1 : -1));
         else if (r.tri < 0) h = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
         else h = make_float4(r.t, r.u, r.v, __int_as_float(r.id));
         hits[i] = h;
+    };
+    if (!COUNT && n < (1ull << 31)) {
+        // The renderer's traversal: persistent lanes with ray replacement;
+        // stats[2] is the queue cursor.
+        traverse_queue<ANY>(
+            S, (uint32_t)n, reinterpret_cast<uint32_t*>(stats + 2),
+            [&](uint32_t i, v3& o, v3& d, float& tmin, float& tmax) -> uint32_t {
+                float4 a = ldg_(rays + 2 * (size_t)i), b = ldg_(rays + 2 * (size_t)i + 1);
+                o = mk(a.x, a.y, a.z);
+                d = mk(b.x, b.y, b.z);
+                tmin = a.w;
+                tmax = b.w;
+                return i;
+            },
+            store);
+        return;
+    }
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float4 a = ldg_(rays + 2 * i), b = ldg_(rays + 2 * i + 1);
+        store(i, COUNT ? traverse<ANY, true>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, nodes, tris)
+                       : traverse_fast<ANY>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w));
     }
     if (COUNT) {
         for (int o = 16; o > 0; o >>= 1) {
@@ -60,7 +78,7 @@ void trace_rays(aqua_ctx* ctx, aqua_scene* sc, const aqua_ray* rays, size_t n, a
     }
     if (!ctx->trace_stats.ptr) dev_alloc(ctx, ctx->trace_stats, 64);
     unsigned long long* d_stats = (unsigned long long*)ctx->trace_stats.ptr;
-    AQ_CUDA(cudaMemsetAsync(d_stats, 0, 16, st));
+    AQ_CUDA(cudaMemsetAsync(d_stats, 0, 24, st));  // node and triangle counters, queue cursor
     auto k = any ? (count ? k_trace_user<true, true> : k_trace_user<true, false>)
                  : (count ? k_trace_user<false, true> : k_trace_user<false, false>);
     int per_sm = 1;
