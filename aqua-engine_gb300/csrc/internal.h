@@ -113,7 +113,7 @@ struct DevJob {
     float* out;              // width * height * 3 floats
     uint64_t seed;
     int32_t scene, spp, max_depth, rr_depth;
-    uint32_t pixels, unit_begin, units, pad;
+    uint32_t pixels, pixel_begin;    // pixels of the job, its first pixel in the batch
 };
 
 // The last batch, kept so an identical batch replays its CUDA graph.
