@@ -76,7 +76,10 @@ class IntegratorCfg(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("slots", "block_trace", "block_shade", "sort_by_material",
-                                         "blocks_per_sm", "use_graph", "iters_per_graph", "replicas")]
+                                         "blocks_per_sm", "use_graph", "iters_per_graph", "replicas", "kernel")]
+
+
+KERNEL_WAVEFRONT, KERNEL_PERSISTENT = 0, 1
 
 
 class Stats(C.Structure):

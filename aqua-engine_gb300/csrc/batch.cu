@@ -286,48 +286,17 @@ void batch_release(aqua_ctx* ctx) {
     g = BatchGraph{};
 }
 
-void render_batch(aqua_ctx* ctx, const aqua_job* in, size_t n, const aqua_tuning& tune, aqua_batch_stats* stats) {
-    if (n == 0) return;
-    if (n > (size_t)kMaxBatchJobs) throw Error(AQUA_ERR_INVALID_ARG, "at most 1024 jobs per batch");
-    std::vector<DevScene> scenes;
-    std::map<const aqua_scene*, int> scene_index;
-    std::vector<DevJob> jobs(n);
-    uint32_t total_pixels = 0;
-    for (size_t i = 0; i < n; ++i) {
-        const aqua_job& j = in[i];
-        if (!j.scene || !j.rgb_out) throw Error(AQUA_ERR_INVALID_ARG, "job " + std::to_string(i) + ": scene and rgb_out must be non-NULL");
-        if (j.width <= 0 || j.height <= 0 || j.width > 16384 || j.height > 16384)
-            throw Error(AQUA_ERR_INVALID_ARG, "job " + std::to_string(i) + ": resolution out of range");
-        if (j.spp <= 0 || j.max_depth < 0 || j.max_depth > 250)
-            throw Error(AQUA_ERR_INVALID_ARG, "job " + std::to_string(i) + ": spp must be > 0 and max_depth in [0, 250]");
-        if (((uintptr_t)j.rgb_out & 3) != 0) throw Error(AQUA_ERR_INVALID_ARG, "rgb_out must be 4-byte aligned");
-        auto it = scene_index.find(j.scene);
-        int si;
-        if (it == scene_index.end()) {
-            si = (int)scenes.size();
-            scene_index[j.scene] = si;
-            scenes.push_back(j.scene->ds);
-        } else {
-            si = it->second;
-        }
-        aqua_camera cam = j.scene->host.cam;
-        cam.width = j.width;
-        cam.height = j.height;
-        DevJob& d = jobs[i];
-        memset(&d, 0, sizeof(d));
-        d.cam = dev_camera(cam);
-        d.out = j.rgb_out;
-        d.seed = j.seed;
-        d.scene = si;
-        d.spp = j.spp;
-        d.max_depth = j.max_depth;
-        d.rr_depth = 3;
-        d.pixels = (uint32_t)j.width * (uint32_t)j.height;
-        d.pixel_begin = total_pixels;
-        if ((uint64_t)total_pixels + d.pixels > 0xFFFFFF00ull)
-            throw Error(AQUA_ERR_INVALID_ARG, "a batch holds at most 2^32 - 256 pixels");
-        total_pixels += d.pixels;
-    }
+// One persistent launch over `jobs` (graph-replayed when the job list
+// repeats): device time, counters and per-job completion clocks.
+struct BatchResult {
+    double ms = 0.0;
+    uint64_t paths = 0, ext = 0, shadow = 0;
+    std::vector<unsigned long long> clocks;
+};
+
+static BatchResult launch_jobs(aqua_ctx* ctx, std::vector<DevJob>& jobs, std::vector<DevScene>& scenes,
+                               uint32_t total_pixels, const aqua_tuning& tune) {
+    const size_t n = jobs.size();
     int block = tune.block_trace > 0 ? tune.block_trace : 128;
     if (block != 64 && block != 128 && block != 256) throw Error(AQUA_ERR_INVALID_ARG, "block size must be 64, 128 or 256");
     int per_sm = tune.blocks_per_sm;
@@ -406,12 +375,111 @@ void render_batch(aqua_ctx* ctx, const aqua_job* in, size_t n, const aqua_tuning
     AQ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    BatchResult r;
+    r.ms = ms;
+    r.paths = hs[0];
+    r.ext = hs[1];
+    r.shadow = hs[2];
+    r.clocks = std::move(clocks);
+    return r;
+}
+
+
+void render_batch(aqua_ctx* ctx, const aqua_job* in, size_t n, const aqua_tuning& tune, aqua_batch_stats* stats) {
+    if (n == 0) return;
+    if (n > (size_t)kMaxBatchJobs) throw Error(AQUA_ERR_INVALID_ARG, "at most 1024 jobs per batch");
+    std::vector<DevScene> scenes;
+    std::map<const aqua_scene*, int> scene_index;
+    std::vector<DevJob> jobs(n);
+    uint32_t total_pixels = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const aqua_job& j = in[i];
+        if (!j.scene || !j.rgb_out) throw Error(AQUA_ERR_INVALID_ARG, "job " + std::to_string(i) + ": scene and rgb_out must be non-NULL");
+        if (j.width <= 0 || j.height <= 0 || j.width > 16384 || j.height > 16384)
+            throw Error(AQUA_ERR_INVALID_ARG, "job " + std::to_string(i) + ": resolution out of range");
+        if (j.spp <= 0 || j.max_depth < 0 || j.max_depth > 250)
+            throw Error(AQUA_ERR_INVALID_ARG, "job " + std::to_string(i) + ": spp must be > 0 and max_depth in [0, 250]");
+        if (((uintptr_t)j.rgb_out & 3) != 0) throw Error(AQUA_ERR_INVALID_ARG, "rgb_out must be 4-byte aligned");
+        auto it = scene_index.find(j.scene);
+        int si;
+        if (it == scene_index.end()) {
+            si = (int)scenes.size();
+            scene_index[j.scene] = si;
+            scenes.push_back(j.scene->ds);
+        } else {
+            si = it->second;
+        }
+        aqua_camera cam = j.scene->host.cam;
+        cam.width = j.width;
+        cam.height = j.height;
+        DevJob& d = jobs[i];
+        memset(&d, 0, sizeof(d));
+        d.cam = dev_camera(cam);
+        d.out = j.rgb_out;
+        d.seed = j.seed;
+        d.scene = si;
+        d.spp = j.spp;
+        d.max_depth = j.max_depth;
+        d.rr_depth = 3;
+        d.pixels = (uint32_t)j.width * (uint32_t)j.height;
+        d.pixel_begin = total_pixels;
+        if ((uint64_t)total_pixels + d.pixels > 0xFFFFFF00ull)
+            throw Error(AQUA_ERR_INVALID_ARG, "a batch holds at most 2^32 - 256 pixels");
+        total_pixels += d.pixels;
+    }
+    BatchResult r = launch_jobs(ctx, jobs, scenes, total_pixels, tune);
     if (stats) {
-        stats->device_ms = ms;
-        stats->paths = hs[0];
+        stats->device_ms = r.ms;
+        stats->paths = r.paths;
         if (stats->job_ms)
             for (size_t i = 0; i < n; ++i)
-                stats->job_ms[i] = clocks[1 + i] >= clocks[0] ? (double)(clocks[1 + i] - clocks[0]) * 1e-6 : -1.0;
+                stats->job_ms[i] = r.clocks[1 + i] >= r.clocks[0] ? (double)(r.clocks[1 + i] - r.clocks[0]) * 1e-6 : -1.0;
+    }
+}
+
+void render_persistent(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, const aqua_tuning& tune,
+                       float* rgb_out, uint32_t flags, aqua_stats* stats) {
+    if (cfg.spp <= 0 || cfg.max_depth < 0 || cfg.max_depth > 250)
+        throw Error(AQUA_ERR_INVALID_ARG, "spp must be > 0 and max_depth in [0, 250]");
+    const aqua_camera& cam = sc->host.cam;
+    const size_t pixels = (size_t)cam.width * (size_t)cam.height;
+    if (pixels == 0 || pixels > 0xFFFFFF00ull) throw Error(AQUA_ERR_INVALID_ARG, "image size out of range");
+    const bool device_film = (flags & AQUA_RENDER_DEVICE_FILM) != 0;
+    float* film = rgb_out;
+    if (!device_film) {
+        if (ctx->persist_film.bytes < 12 * pixels) {
+            dev_free(ctx->persist_film);
+            dev_alloc(ctx, ctx->persist_film, 12 * pixels);
+        }
+        film = (float*)ctx->persist_film.ptr;
+    } else if (((uintptr_t)rgb_out & 3) != 0) {
+        throw Error(AQUA_ERR_INVALID_ARG, "rgb_out must be 4-byte aligned");
+    }
+    std::vector<DevScene> scenes{sc->ds};
+    std::vector<DevJob> jobs(1);
+    DevJob& d = jobs[0];
+    memset(&d, 0, sizeof(d));
+    d.cam = dev_camera(cam);
+    d.out = film;
+    d.seed = cfg.seed;
+    d.scene = 0;
+    d.spp = cfg.spp;
+    d.max_depth = cfg.max_depth;
+    d.rr_depth = cfg.rr_depth;
+    d.pixels = (uint32_t)pixels;
+    d.pixel_begin = 0;
+    BatchResult r = launch_jobs(ctx, jobs, scenes, (uint32_t)pixels, tune);
+    if (!device_film) {
+        AQ_CUDA(cudaMemcpyAsync(rgb_out, film, 12 * pixels, cudaMemcpyDeviceToHost, ctx->stream));
+        AQ_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->paths = r.paths;
+        stats->ext_rays = r.ext;
+        stats->shadow_rays = r.shadow;
+        stats->device_ms = r.ms;
+        stats->total_launches = 1;
     }
 }
 

@@ -286,6 +286,7 @@ AQUA_API void aqua_destroy(aqua_ctx* ctx) {
     dev_free(ctx->nrc_ws.block);
     dev_free(ctx->trace_rays);
     dev_free(ctx->trace_hits);
+    dev_free(ctx->persist_film);
     dev_free(ctx->trace_stats);
     for (auto e : ctx->events) cudaEventDestroy(e);
     if (ctx->pinned_counter) cudaFreeHost(ctx->pinned_counter);
@@ -521,12 +522,19 @@ AQUA_API aqua_status aqua_render(aqua_ctx* ctx, aqua_scene* s, const aqua_integr
         else aqua_tuning_defaults(&t);
         if (cfg->type != AQUA_INTEGRATOR_PATH)
             throw Error(AQUA_ERR_UNSUPPORTED, "integrator type not available in aqua_render");
-        render_path(ctx, s, *cfg, t, rgb_out, flags, stats);
+        need(t.kernel == AQUA_KERNEL_WAVEFRONT || t.kernel == AQUA_KERNEL_PERSISTENT,
+             "tuning.kernel must be an AQUA_KERNEL_* value");
+        const uint32_t wavefront_only = AQUA_RENDER_COUNT | AQUA_RENDER_STAGE_TIMING | AQUA_RENDER_ACCUMULATE;
+        if (t.kernel == AQUA_KERNEL_PERSISTENT && !(flags & wavefront_only) && cfg->spp_offset == 0)
+            render_persistent(ctx, s, *cfg, t, rgb_out, flags, stats);
+        else
+            render_path(ctx, s, *cfg, t, rgb_out, flags, stats);
     });
 }
 
 // Autotuner: times short renders (at most 16 spp) of every candidate launch
-// shape, two runs each, and keeps the fastest by device time.
+// shape of both integrator kernels (wavefront, persistent), two runs each,
+// and keeps the fastest by device time.
 AQUA_API aqua_status aqua_autotune(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg* cfg, aqua_tuning* out) {
     return guard(ctx, [&]() {
         need(s && cfg && out, "scene, cfg and out must be non-NULL");
@@ -563,6 +571,25 @@ AQUA_API aqua_status aqua_autotune(aqua_ctx* ctx, aqua_scene* s, const aqua_inte
                                 best = t;
                             }
                         }
+            // The persistent kernel: block size x resident blocks.
+            for (int block : {128, 256})
+                for (int bps : {0, 4, 8}) {
+                    aqua_tuning t;
+                    aqua_tuning_defaults(&t);
+                    t.kernel = AQUA_KERNEL_PERSISTENT;
+                    t.block_trace = block;
+                    t.blocks_per_sm = bps;
+                    double ms = 0.0;
+                    for (int rep = 0; rep < 2; ++rep) {
+                        aqua_stats st;
+                        render_persistent(ctx, s, c, t, (float*)film.ptr, AQUA_RENDER_DEVICE_FILM, &st);
+                        if (rep == 1) ms = st.device_ms;
+                    }
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        best = t;
+                    }
+                }
         } catch (...) {
             dev_free(film);
             throw;

@@ -169,6 +169,7 @@ struct aqua_ctx {
     unsigned int* pinned_counter = nullptr;  // host-mapped copy of queue counts
     std::vector<cudaEvent_t> events;         // pool for stage timing
     aq::DevBuf trace_rays, trace_hits;       // staging for host-pointer traces
+    aq::DevBuf persist_film;                 // device film of host-film persistent renders
     aq::DevBuf trace_stats;
 };
 
@@ -197,6 +198,9 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg& cfg, co
 
 // Batched rendering (batch.cu).
 void render_batch(aqua_ctx* ctx, const aqua_job* jobs, size_t n, const aqua_tuning& tune, aqua_batch_stats* stats);
+// One image with the batch kernel (AQUA_KERNEL_PERSISTENT).
+void render_persistent(aqua_ctx* ctx, aqua_scene* s, const aqua_integrator_cfg& cfg, const aqua_tuning& tune,
+                       float* rgb_out, uint32_t flags, aqua_stats* stats);
 void batch_release(aqua_ctx* ctx);
 
 // Radiance-cache network (nrc.cu).

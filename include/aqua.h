@@ -123,7 +123,18 @@ typedef struct aqua_tuning {
     int32_t replicas;       /* sample replicas per pixel: 0 = automatic (small
                                images get several slots per pixel, each with
                                its own film copy), 1 = off, k = k copies     */
+    int32_t kernel;         /* AQUA_KERNEL_*: the wavefront (three launches per
+                               bounce over compacted, material-sorted queues)
+                               or one persistent launch whose lanes each keep a
+                               path in flight and regenerate it in place (the
+                               aqua_render_batch kernel; block_trace and
+                               blocks_per_sm shape it). Same image either way.
+                               Renders with AQUA_RENDER_COUNT, _STAGE_TIMING or
+                               _ACCUMULATE, or a non-zero spp_offset, run on the
+                               wavefront. aqua_autotune times both.           */
 } aqua_tuning;
+
+enum { AQUA_KERNEL_WAVEFRONT = 0, AQUA_KERNEL_PERSISTENT = 1 };
 
 typedef struct aqua_stats {
     uint64_t paths;          /* camera paths completed                       */

@@ -142,6 +142,52 @@ def test_invalid_arguments_raise(gpu_ctx):
     s.free()
 
 
+@pytest.mark.parametrize("config", [2, 3])
+def test_persistent_kernel_matches_wavefront(gpu_ctx, config):
+    """The persistent kernel (one launch, a path per lane regenerated in
+    place) renders the same image as the wavefront: same random numbers per
+    sample and bounce, contributions summed per pixel in the same order, so
+    only the per-pixel film summation (one sum vs film += per event) differs.
+    Ray counts are equal."""
+    import aqua
+    import pyoracle
+
+    s = gpu_ctx.procedural(config, seed=0, width=64, height=48)
+    cfg = gpu_ctx.integrator(spp=32, max_depth=8, rr_depth=3, seed=5)
+    wf, sw = gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning(kernel=aqua.KERNEL_WAVEFRONT))
+    pk, sp = gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning(kernel=aqua.KERNEL_PERSISTENT))
+    np.testing.assert_allclose(pk, wf, rtol=1e-5, atol=1e-6)
+    assert sp.paths == sw.paths == 64 * 48 * 32
+    assert (sp.ext_rays, sp.shadow_rays) == (sw.ext_rays, sw.shadow_rays)
+    assert sp.total_launches == 1 and sp.iterations == 0
+    again, _ = gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning(kernel=aqua.KERNEL_PERSISTENT, block_trace=256,
+                                                            blocks_per_sm=2))
+    assert np.array_equal(again, pk)  # the launch shape does not change the image
+    # Flags the persistent kernel does not serve run on the wavefront.
+    _, sc = gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning(kernel=aqua.KERNEL_PERSISTENT), flags=aqua.RENDER_COUNT)
+    assert sc.node_visits > 0 and sc.iterations > 0
+    o = pyoracle.OracleScene.from_aqua(s)
+    ref, _ = o.render(32, 8, seed=5, precision=64)
+    assert pyoracle.rel_mse(pk, ref) < TOL
+    s.free()
+
+
+def test_autotune_picks_a_kernel(gpu_ctx):
+    import aqua
+
+    s = gpu_ctx.procedural(2, seed=0, width=96, height=64)
+    cfg = gpu_ctx.integrator(spp=64, max_depth=8, rr_depth=3, seed=3)
+    t = gpu_ctx.autotune(s, cfg)
+    assert t.kernel in (aqua.KERNEL_WAVEFRONT, aqua.KERNEL_PERSISTENT)
+    img, st = gpu_ctx.render(s, cfg, tuning=t)
+    ref, _ = gpu_ctx.render(s, cfg)
+    np.testing.assert_allclose(img, ref, rtol=1e-5, atol=1e-6)
+    with pytest.raises(aqua.AquaError) as e:
+        gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning(kernel=7))
+    assert e.value.status == aqua.ERR_INVALID_ARG
+    s.free()
+
+
 def test_stats_and_stage_timing(gpu_ctx):
     import aqua
 
