@@ -285,6 +285,9 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
     unsigned long long done_paths = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t s;
+        // With sorted queues the bucket is the material, so its parameters
+        // load alongside the path state instead of after the triangle.
+        float4 mat_a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), mat_b = mat_a;
         if (SORTED) {
             uint32_t lo = 0, hi = P.nb - 1;
             while (lo < hi) {  // last bucket b with prefix[b] <= i
@@ -293,6 +296,11 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                 else hi = mid - 1;
             }
             s = W.bucket[(size_t)lo * P.slots + (i - prefix[lo])];
+            if (lo + 1 < P.nb) {  // the last bucket holds the misses
+                const float4* mp = reinterpret_cast<const float4*>(S.mats + lo);
+                mat_a = ldg_(mp);
+                mat_b = ldg_(mp + 1);
+            }
         } else {
             s = W.q_in[i];
         }
@@ -342,7 +350,13 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
             const int depth_limit = (NRC && tag) ? P.train_depth : P.max_depth;
             if ((int)depth < depth_limit) {
                 if (dot(ng, wo) < 0.0f) ng = -ng;
-                DevMaterial m = S.mats[info & 0xffffu];
+                DevMaterial m;
+                if (SORTED) {
+                    m.a = mat_a;
+                    m.b = mat_b;
+                } else {
+                    m = S.mats[info & 0xffffu];
+                }
                 v3 base = f3(m.a);
                 int ti = __float_as_int(m.a.w);
                 if (ti >= 0) {
