@@ -318,7 +318,9 @@ def run_interior_metric(ctx, warmup: int = 1, steps: int = 2):
         ctx.render_device(scene, cfg, film.data_ptr())
     ms, paths, rays = 0.0, 0, 0
     for _ in range(steps):
+        torch.cuda.nvtx.range_push("interior_step")
         st = ctx.render_device(scene, cfg, film.data_ptr())
+        torch.cuda.nvtx.range_pop()
         ms += st.device_ms
         paths += st.paths
         rays += st.ext_rays + st.shadow_rays
@@ -384,7 +386,7 @@ BATCH_WORKLOAD = {"workload": "batch-64-jobs-4-scenes",
                   "spp_distribution": "log-uniform, seed 5", "max_depth": 8}
 
 
-def run_batch_metric(ctx, warmup: int = 1, steps: int = 2):
+def run_batch_metric(ctx, warmup: int = 1, steps: int = 2, spp_div: int = 1):
     """64 jobs over 4 seeded scenes in one persistent launch per step:
     aggregate Mpaths/s and per-job completion latency p50/p99."""
     import numpy as np
@@ -399,7 +401,7 @@ def run_batch_metric(ctx, warmup: int = 1, steps: int = 2):
     for i in range(W["jobs"]):
         res = int(rng.choice(W["resolutions"]))
         spp = int(round(np.exp(rng.uniform(np.log(16), np.log(1024)))))
-        specs.append((int(rng.integers(0, 4)), res, res, spp, W["max_depth"], 1000 + i))
+        specs.append((int(rng.integers(0, 4)), res, res, max(1, spp // spp_div), W["max_depth"], 1000 + i))
     bufs = [torch.empty(r * r * 3, dtype=torch.float32, device="cuda") for (_, r, _, _, _, _) in specs]
     jobs = [(scenes[s], w, h, spp, d, seed, b.data_ptr()) for (s, w, h, spp, d, seed), b in zip(specs, bufs)]
     torch.cuda.synchronize()
@@ -410,7 +412,9 @@ def run_batch_metric(ctx, warmup: int = 1, steps: int = 2):
         ctx.render_batch(jobs, tune)
     ms, paths, lat = 0.0, 0, []
     for _ in range(steps):
+        torch.cuda.nvtx.range_push("batch_step")
         st, job_ms = ctx.render_batch(jobs, tune)
+        torch.cuda.nvtx.range_pop()
         ms += st.device_ms
         paths += st.paths
         lat.extend(job_ms.tolist())
@@ -537,7 +541,9 @@ def run_gpu(args, world, rank, local, pg):
         nrc = run_nrc_metric(ctx, args.nrc_budget)
     batch = None
     if rank == 0 and not args.no_batch:
-        batch = run_batch_metric(ctx)
+        batch = run_batch_metric(ctx, spp_div=args.batch_spp_div)
+        if args.batch_spp_div != 1:
+            batch["config"] = dict(batch["config"], spp_divided_by=args.batch_spp_div)
     nrc_inf = None
     if rank == 0 and not args.no_nrc:
         bf16_peak = peaks.get("bf16_tflops", 1900.0)
@@ -591,6 +597,8 @@ def main():
                     help="rows of the cache-inference measurement (smaller only for profiling captures)")
     ap.add_argument("--nrc-budget", type=float, default=60.0, help="seconds per arm of that measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-job batched-serving measurement")
+    ap.add_argument("--batch-spp-div", type=int, default=1,
+                    help="divide every batch job's spp by this (profiling captures only)")
     ap.add_argument("--no-interior", action="store_true", help="skip the 1080p interior measurement")
     # dram__bytes_read.sum + dram__bytes_write.sum of one full-queue
     # k_trace_ext launch (1M rays) of this workload, from `ncu --set full`
