@@ -3,6 +3,7 @@
 #include "scene.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <fstream>
@@ -298,16 +299,22 @@ struct Bsdf_ {
     v3 emission;
 };
 
-// Decoded `Image` textures by file, so materials that share a file share a
-// texture. Texture rows are stored bottom-up (row 0 = the image's last row):
-// v = 0 is the bottom edge of the image, as in the OBJ texture coordinates
-// the .mesh files carry.
+// `Image` textures by file, so materials that share a file share a texture.
+// Files are only checked while the JSON is read; decoding runs afterwards on
+// all host threads (decode_textures). Texture rows are stored bottom-up
+// (row 0 = the image's last row): v = 0 is the bottom edge of the image, as
+// in the OBJ texture coordinates the .mesh files carry.
 struct TexCache {
     HostScene& s;
     std::map<std::string, int> index;
+    struct Pending {
+        int tex;
+        std::string path, bsdf;
+    };
+    std::vector<Pending> pending;
 };
 
-// Index of the decoded texture, or -1 when it is missing or undecodable and
+// Index of the texture for `full`, or -1 when the file is missing and
 // allow_missing is set (the caller then uses mid-grey).
 int image_texture(TexCache& tc, const std::string& full, bool allow_missing, const std::string& name) {
     auto it = tc.index.find(full);
@@ -317,29 +324,58 @@ int image_texture(TexCache& tc, const std::string& full, bool allow_missing, con
         if (allow_missing) return tc.index[full] = -1;
         throw SceneError(AQUA_ERR_MISSING_ASSET, "bsdf \"" + name + "\": texture " + full + " is missing");
     }
-    std::vector<uint8_t> data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
-    JpegImage img;
-    std::string err = jpeg_decode(data.data(), data.size(), img);
-    if (!err.empty()) {
-        if (allow_missing) return tc.index[full] = -1;
-        throw SceneError(AQUA_ERR_UNSUPPORTED, "bsdf \"" + name + "\": texture " + full + ": " + err);
-    }
-    Texture t;
-    t.w = img.w;
-    t.h = img.h;
-    t.rgba.resize((size_t)img.w * (size_t)img.h * 4);
-    for (int y = 0; y < img.h; ++y) {
-        const uint8_t* src = &img.rgb[(size_t)(img.h - 1 - y) * (size_t)img.w * 3];
-        uint8_t* dst = &t.rgba[(size_t)y * (size_t)img.w * 4];
-        for (int x = 0; x < img.w; ++x) {
-            dst[4 * x] = src[3 * x];
-            dst[4 * x + 1] = src[3 * x + 1];
-            dst[4 * x + 2] = src[3 * x + 2];
-            dst[4 * x + 3] = 255;
+    tc.s.textures.push_back(Texture{});
+    const int ti = (int)tc.s.textures.size() - 1;
+    tc.pending.push_back({ti, full, name});
+    return tc.index[full] = ti;
+}
+
+// Decodes the pending textures in parallel. A file the decoder refuses fails
+// the load with AQUA_ERR_UNSUPPORTED, or with allow_missing becomes a 1x1
+// texture of linear 0.5 (the mid-grey stand-in).
+void decode_textures(TexCache& tc, bool allow_missing) {
+    const size_t n = tc.pending.size();
+    std::vector<std::string> errs(n);
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (size_t k = next++; k < n; k = next++) {
+            const TexCache::Pending& p = tc.pending[k];
+            std::ifstream f(p.path, std::ios::binary);
+            std::vector<uint8_t> data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+            JpegImage img;
+            errs[k] = jpeg_decode(data.data(), data.size(), img);
+            Texture& t = tc.s.textures[(size_t)p.tex];
+            if (!errs[k].empty()) {
+                t.w = t.h = 1;
+                t.rgba = {188, 188, 188, 255};  // sRGB encoding of linear 0.5
+                continue;
+            }
+            t.w = img.w;
+            t.h = img.h;
+            t.rgba.resize((size_t)img.w * (size_t)img.h * 4);
+            for (int y = 0; y < img.h; ++y) {
+                const uint8_t* src = &img.rgb[(size_t)(img.h - 1 - y) * (size_t)img.w * 3];
+                uint8_t* dst = &t.rgba[(size_t)y * (size_t)img.w * 4];
+                for (int x = 0; x < img.w; ++x) {
+                    dst[4 * x] = src[3 * x];
+                    dst[4 * x + 1] = src[3 * x + 1];
+                    dst[4 * x + 2] = src[3 * x + 2];
+                    dst[4 * x + 3] = 255;
+                }
+            }
         }
-    }
-    tc.s.textures.push_back(std::move(t));
-    return tc.index[full] = (int)tc.s.textures.size() - 1;
+    };
+    const size_t threads = std::min<size_t>(n, std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (size_t i = 1; i < threads; ++i) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    if (!allow_missing)
+        for (size_t k = 0; k < n; ++k)
+            if (!errs[k].empty())
+                throw SceneError(AQUA_ERR_UNSUPPORTED, "bsdf \"" + tc.pending[k].bsdf + "\": texture " +
+                                                           tc.pending[k].path + ": " + errs[k]);
+    tc.pending.clear();
 }
 
 Bsdf_ read_bsdf(const Json& j, const std::string& dir, bool allow_missing, const std::string& name,
@@ -522,6 +558,7 @@ HostScene load_scene_json(const std::string& path, bool allow_missing) {
     } catch (JsonError& e) {
         throw SceneError(AQUA_ERR_PARSE, path + ": " + e.what());
     }
+    decode_textures(tc, allow_missing);
     finalize_lights(s);
     return s;
 }

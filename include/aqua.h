@@ -238,11 +238,11 @@ AQUA_API int aqua_version(void);
  * lights, shapes) with its BSON meshes from the JSON's directory. A missing
  * mesh (e.g. living_room_Default_43.mesh, .MISSING_LARGE_BLOBS:1) fails with
  * AQUA_ERR_MISSING_ASSET unless allow_missing is set, which skips it. Image
- * textures (room.json:6) are decoded by the built-in JPEG decoder (Huffman
- * sequential and progressive, 8-bit, grey or YCbCr); a file it refuses
- * (arithmetic coding, 12-bit, lossless) fails with AQUA_ERR_UNSUPPORTED and a
- * missing file with AQUA_ERR_MISSING_ASSET, unless allow_missing is set, which
- * replaces the texture by mid-grey. Texture rows are stored bottom-up, so
+ * textures (room.json:6) are decoded, on all host threads, by the built-in
+ * JPEG decoder (Huffman sequential and progressive, 8-bit, grey or YCbCr); a
+ * file it refuses (arithmetic coding, 12-bit, lossless) fails with
+ * AQUA_ERR_UNSUPPORTED and a missing file with AQUA_ERR_MISSING_ASSET, unless
+ * allow_missing is set, which replaces the texture by mid-grey. Texture rows are stored bottom-up, so
  * v = 0 is the bottom edge of the image (OBJ texture coordinates). */
 AQUA_API aqua_status aqua_load_scene_json(aqua_ctx* ctx, const char* path,
                                           int32_t allow_missing, aqua_scene** out);

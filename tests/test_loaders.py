@@ -79,6 +79,45 @@ def quad_scene(tmp_path):
 
 
 # ---------------------------------------------------------------- synthetic
+def test_image_textures(host_ctx, quad_scene):
+    """`Image` colours (room.json:6): JPEG files decode to bottom-up RGBA8
+    textures shared per file; a file the decoder refuses fails the load, or
+    with allow_missing becomes a 1x1 linear-0.5 texture; a missing file
+    fails, or with allow_missing leaves the material mid-grey untextured."""
+    import sys
+
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    import test_jpeg
+
+    d, p = quad_scene
+    img = test_jpeg.synthetic_image(12, 20, 4)
+    data, expect = test_jpeg.encode(img)
+    (d / "t.jpg").write_bytes(data)
+    (d / "bad.jpg").write_bytes(b"\x89PNG\r\n\x1a\n" + bytes(64))
+    bsdfs = {"a": principled({"Image": "t.jpg"}), "b": principled({"Image": "t.jpg"}),
+             "c": principled({"Image": "bad.jpg"}), "d": principled({"Image": "gone.jpg"})}
+    shapes = [("quad.mesh", k) for k in bsdfs]
+    p.write_text(json.dumps(scene_json(shapes, bsdfs)))
+    with pytest.raises(aqua.AquaError) as e:
+        host_ctx.load_scene(str(p))
+    assert e.value.status in (aqua.ERR_UNSUPPORTED, aqua.ERR_MISSING_ASSET)
+    s = host_ctx.load_scene(str(p), allow_missing=True)
+    assert s.info().num_textures == 2  # t.jpg once, bad.jpg as the stand-in
+    mats = s.materials()
+    assert mats[0].base_texture == mats[1].base_texture == 0 and list(mats[0].base_color) == [1.0, 1.0, 1.0]
+    t0 = s.texture(0)
+    assert t0.shape == (12, 20, 4)
+    np.testing.assert_array_equal(t0[::-1, :, :3], expect)  # stored bottom-up
+    assert mats[2].base_texture == 1 and s.texture(1).tolist() == [[[188, 188, 188, 255]]]
+    assert mats[3].base_texture == -1 and abs(mats[3].base_color[0] - 0.5) < 1e-7
+    s.free()
+    del bsdfs["d"]
+    p.write_text(json.dumps(scene_json([("quad.mesh", k) for k in bsdfs], bsdfs)))
+    with pytest.raises(aqua.AquaError) as e:
+        host_ctx.load_scene(str(p))
+    assert e.value.status == aqua.ERR_UNSUPPORTED and "bad.jpg" in str(e.value)
+
+
 def test_synthetic_scene_loads(host_ctx, quad_scene):
     d, p = quad_scene
     s = host_ctx.load_scene(str(p))
