@@ -166,6 +166,7 @@ SIGNATURES = [
     ("aqua_nrc_encode", C.c_int, [_P, _P, _P, C.c_size_t, _P, C.c_uint32]),
     ("aqua_nrc_forward", C.c_int, [_P, _P, _P, C.c_size_t, _P, C.c_uint32]),
     ("aqua_nrc_last_ms", C.c_int, [_P, _P, C.POINTER(C.c_float)]),
+    ("aqua_scene_export_normals", C.c_int, [_P, _P, _P, C.POINTER(C.c_int32)]),
     ("aqua_decode_jpeg", C.c_int, [_P, _P, C.c_size_t, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P]),
     ("aqua_convert_obj", C.c_int, [_P, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32,
                                    C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
@@ -311,6 +312,18 @@ class Scene:
         self.ctx._check(self.ctx.lib.aqua_scene_export_triangles(self.ctx.handle, self.handle, _ptr(v), _ptr(uv),
                                                                  _ptr(m), _ptr(li)))
         return v, uv, m, li
+
+    def normals(self):
+        """(n, 9) float32 vertex normals per triangle, or None for a flat-shaded scene."""
+        present = C.c_int32()
+        self.ctx._check(self.ctx.lib.aqua_scene_export_normals(self.ctx.handle, self.handle, None,
+                                                               C.byref(present)))
+        if not present.value:
+            return None
+        out = np.zeros((self.info().num_triangles, 9), np.float32)
+        self.ctx._check(self.ctx.lib.aqua_scene_export_normals(self.ctx.handle, self.handle, _ptr(out),
+                                                               C.byref(present)))
+        return out
 
     def camera(self) -> Camera:
         c = Camera()

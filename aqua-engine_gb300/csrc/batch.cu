@@ -99,6 +99,7 @@ __device__ __forceinline__ bool bounce(const DevScene& S, int max_depth, int rr_
         }
         if (depth >= max_depth) return false;
         if (dot(ng, wo) < 0.0f) ng = -ng;
+        const v3 ns = shading_normal(S, h.tri, h.u, h.v, ng, wo);
         DevMaterial m = S.mats[info & 0xffffu];
         v3 base = f3(m.a);
         int ti = __float_as_int(m.a.w);
@@ -112,8 +113,8 @@ __device__ __forceinline__ bool bounce(const DevScene& S, int max_depth, int rr_
         }
         Bsdf B = make_bsdf(base, m.b.x, m.b.y, m.b.z);
         v3 T, Bt;
-        onb(ng, T, Bt);
-        v3 wol = mk(dot(wo, T), dot(wo, Bt), dot(wo, ng));
+        onb(ns, T, Bt);
+        v3 wol = mk(dot(wo, T), dot(wo, Bt), dot(wo, ns));
         float u[kBounceDims];
 #pragma unroll
         for (int k = 0; k < kBounceDims; ++k) u[k] = draw(st, inc);
@@ -128,8 +129,8 @@ __device__ __forceinline__ bool bounce(const DevScene& S, int max_depth, int rr_
                 float d2 = dot(dl, dl);
                 dist = sqrtf(d2);
                 wi = dl * (1.0f / dist);
-                float cs = dot(wi, ng);
-                if (cs > 0.0f && d2 > 0.0f) {
+                float cs = dot(wi, ns), cg = dot(wi, ng);
+                if (cs > 0.0f && cg > 0.0f && d2 > 0.0f) {
                     v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
                     contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs / (d2 * pmf));
                 }
@@ -146,8 +147,8 @@ __device__ __forceinline__ bool bounce(const DevScene& S, int max_depth, int rr_
                 float d2 = dot(dl, dl);
                 dist = sqrtf(d2);
                 wi = dl * (1.0f / dist);
-                float cl = -dot(wi, nl), cs = dot(wi, ng);
-                if (cl > 0.0f && cs > 0.0f && d2 > 0.0f) {
+                float cl = -dot(wi, nl), cs = dot(wi, ns), cg = dot(wi, ng);
+                if (cl > 0.0f && cs > 0.0f && cg > 0.0f && d2 > 0.0f) {
                     v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
                     float pl = pmf * d2 / (L.e1.w * cl);
                     float pb = bsdf_pdf(B, wol, wil);
@@ -175,7 +176,8 @@ __device__ __forceinline__ bool bounce(const DevScene& S, int max_depth, int rr_
             else thr = thr * (1.0f / q);
         }
         if (!ok) return false;
-        dir = normalize(T * wil.x + Bt * wil.y + ng * wil.z);
+        dir = normalize(T * wil.x + Bt * wil.y + ns * wil.z);
+        if (S.nrm && !(dot(dir, ng) > 0.0f)) return false;  // below the geometric surface
         o = offset_ray(p, ng);
         pdf_b = pdf;
         P.depth = depth + 1;

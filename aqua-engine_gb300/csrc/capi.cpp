@@ -87,7 +87,8 @@ void scene_build_device(aqua_ctx* ctx, aqua_scene* s) {
     size_t o_nodes = 0, o_tris = align256(o_nodes + 64 * nn), o_uvs = align256(o_tris + 48 * nt),
            o_mats = align256(o_uvs + 24 * nt), o_lights = align256(o_mats + 32 * h.mats.size()),
            o_texs = align256(o_lights + 64 * h.lights.size()),
-           o_texels = align256(o_texs + 16 * h.textures.size()), total = align256(o_texels + 4 * texels);
+           o_texels = align256(o_texs + 16 * h.textures.size()), o_nrm = align256(o_texels + 4 * texels),
+           total = align256(o_nrm + (h.nrm.empty() ? 0 : 48 * nt));
     free_staging(s);
     if (ctx->host_only) {
         s->pinned = malloc(total);
@@ -102,8 +103,12 @@ void scene_build_device(aqua_ctx* ctx, aqua_scene* s) {
     memcpy(p + o_nodes, s->bvh.nodes.data(), 64 * nn);
     float* tw = (float*)(p + o_tris);
     float* uw = (float*)(p + o_uvs);
+    float* nw = h.nrm.empty() ? nullptr : (float*)(p + o_nrm);
     for (size_t k = 0; k < nt; ++k) {
         int32_t i = s->bvh.tri_order[k];
+        if (nw)
+            for (int c = 0; c < 3; ++c)
+                for (int a = 0; a < 3; ++a) nw[12 * k + 4 * (size_t)c + (size_t)a] = h.nrm[9 * (size_t)i + 3 * (size_t)c + (size_t)a];
         const float* v = &h.verts[9 * (size_t)i];
         uint32_t info = (uint32_t)h.tri_mat[(size_t)i] | ((uint32_t)(h.tri_light[(size_t)i] + 1) << 16);
         float* o = tw + 12 * k;
@@ -160,6 +165,7 @@ void scene_build_device(aqua_ctx* ctx, aqua_scene* s) {
     ds.lights = (const DevLight*)(d + o_lights);
     ds.texs = (const DevTexture*)(d + o_texs);
     ds.texels = (const uint32_t*)(d + o_texels);
+    ds.nrm = h.nrm.empty() ? nullptr : (const float4*)(d + o_nrm);
     ds.n_nodes = (int32_t)nn;
     ds.n_tris = (int32_t)nt;
     ds.n_mats = (int32_t)h.mats.size();
@@ -454,6 +460,14 @@ AQUA_API aqua_status aqua_write_image(aqua_ctx* ctx, const char* path, const flo
         need(path && rgb, "path and rgb must be non-NULL");
         need(width > 0 && height > 0, "width and height must be positive");
         write_image(path, rgb, width, height);
+    });
+}
+
+AQUA_API aqua_status aqua_scene_export_normals(aqua_ctx* ctx, const aqua_scene* s, float* nrm, int32_t* present) {
+    return guard(ctx, [&]() {
+        need(s != nullptr, "scene is NULL");
+        if (present) *present = s->host.nrm.empty() ? 0 : 1;
+        if (nrm && !s->host.nrm.empty()) memcpy(nrm, s->host.nrm.data(), 4 * s->host.nrm.size());
     });
 }
 

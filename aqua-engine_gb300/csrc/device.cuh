@@ -38,6 +38,7 @@ struct DevScene {
     const DevLight* __restrict__ lights;
     const DevTexture* __restrict__ texs;
     const uint32_t* __restrict__ texels;  // RGBA8, sRGB
+    const float4* __restrict__ nrm;    // 3 vertex normals per triangle (xyz, 0), leaf order; null = flat
     int32_t n_nodes, n_tris, n_mats, n_lights, n_texs;
     float env[3];
     DevCamera cam;

@@ -350,6 +350,7 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
             const int depth_limit = (NRC && tag) ? P.train_depth : P.max_depth;
             if ((int)depth < depth_limit) {
                 if (dot(ng, wo) < 0.0f) ng = -ng;
+                const v3 ns = shading_normal(S, tri, h.y, h.z, ng, wo);
                 DevMaterial m;
                 if (SORTED) {
                     m.a = mat_a;
@@ -374,7 +375,7 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                     if (!tag && (int)depth == P.query_depth) {
                         uint32_t k = warp_append(&W.counters[kCntQuery], true);
                         W.q_pix[k] = make_float4(__int_as_float((int)pixel), thr.x, thr.y, thr.z);
-                        nrc_raw(W.q_raw + 16 * (size_t)k, p, wo, ng, m.b.y, kd, B.F0);
+                        nrc_raw(W.q_raw + 16 * (size_t)k, p, wo, ns, m.b.y, kd, B.F0);
                         queried = true;
                     } else if (tag) {
                         float4 lb = W.ltrain[train_id];
@@ -382,7 +383,7 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                         uint32_t k = (int)depth < P.max_depth ? atomicAdd(&W.counters[kCntRecord], 1u) : 0xffffffffu;
                         if (k < P.max_records) {
                             float r[24];
-                            nrc_raw(r, p, wo, ng, m.b.y, kd, B.F0);
+                            nrc_raw(r, p, wo, ns, m.b.y, kd, B.F0);
                             r[16] = thr.x; r[17] = thr.y; r[18] = thr.z;
                             r[19] = lb.x; r[20] = lb.y; r[21] = lb.z;
                             r[22] = __int_as_float((int)train_id);
@@ -395,8 +396,8 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                     }
                 }
                 v3 T, Bt;
-                onb(ng, T, Bt);
-                v3 wol = mk(dot(wo, T), dot(wo, Bt), dot(wo, ng));
+                onb(ns, T, Bt);
+                v3 wol = mk(dot(wo, T), dot(wo, Bt), dot(wo, ns));
                 float u[kBounceDims];
 #pragma unroll
                 for (int k = 0; k < kBounceDims; ++k) u[k] = queried ? 0.0f : draw(st, inc);
@@ -412,8 +413,8 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                         float d2 = dot(dl, dl);
                         dist = sqrtf(d2);
                         wi = dl * (1.0f / dist);
-                        float cs = dot(wi, ng);
-                        if (cs > 0.0f && d2 > 0.0f) {
+                        float cs = dot(wi, ns), cg = dot(wi, ng);
+                        if (cs > 0.0f && cg > 0.0f && d2 > 0.0f) {
                             v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
                             contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs / (d2 * pmf));
                         }
@@ -430,8 +431,8 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                         float d2 = dot(dl, dl);
                         dist = sqrtf(d2);
                         wi = dl * (1.0f / dist);
-                        float cl = -dot(wi, nl), cs = dot(wi, ng);
-                        if (cl > 0.0f && cs > 0.0f && d2 > 0.0f) {
+                        float cl = -dot(wi, nl), cs = dot(wi, ns), cg = dot(wi, ng);
+                        if (cl > 0.0f && cs > 0.0f && cg > 0.0f && d2 > 0.0f) {
                             v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
                             float pl = pmf * d2 / (L.e1.w * cl);
                             float pb = bsdf_pdf(B, wol, wil);
@@ -461,8 +462,9 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                             if (u[6] >= q) ok = false;
                             else thr = thr * (1.0f / q);
                         }
+                        v3 wi = normalize(T * wil.x + Bt * wil.y + ns * wil.z);
+                        if (S.nrm && !(dot(wi, ng) > 0.0f)) ok = false;  // below the geometric surface
                         if (ok) {
-                            v3 wi = normalize(T * wil.x + Bt * wil.y + ng * wil.z);
                             v3 no = offset_ray(p, ng);
                             W.ray_o[s] = make_float4(no.x, no.y, no.z, 0.0f);
                             W.ray_d[s] = make_float4(wi.x, wi.y, wi.z, INFINITY);

@@ -444,6 +444,7 @@ HostScene load_scene_json(const std::string& path, bool allow_missing) {
     if (slash != std::string::npos) dir = path.substr(0, slash);
     HostScene s;
     TexCache tc{s, {}};
+    bool any_normals = false;
     std::vector<v3> mat_emission;
     try {
         Json root = json_parse(text);
@@ -527,9 +528,12 @@ HostScene load_scene_json(const std::string& path, bool allow_missing) {
             bool emissive = em.x > 0 || em.y > 0 || em.z > 0;
             size_t ntri = md.indices.size() / 3;
             bool has_uv = !md.texcoords.empty();
+            const bool has_n = !md.normals.empty();
+            any_normals = any_normals || has_n;
             for (size_t k = 0; k < ntri; ++k) {
                 v3 P[3];
                 float uv[6] = {0, 0, 0, 0, 0, 0};
+                float nv[9];
                 for (int c = 0; c < 3; ++c) {
                     size_t vi = (size_t)md.indices[3 * k + c];
                     P[c] = mk((float)md.positions[3 * vi], (float)md.positions[3 * vi + 1],
@@ -538,7 +542,21 @@ HostScene load_scene_json(const std::string& path, bool allow_missing) {
                         uv[2 * c] = (float)md.texcoords[2 * vi];
                         uv[2 * c + 1] = (float)md.texcoords[2 * vi + 1];
                     }
+                    for (int a = 0; a < 3; ++a) nv[3 * c + a] = has_n ? (float)md.normals[3 * vi + (size_t)a] : 0.0f;
                 }
+                if (!has_n) {  // a flat mesh among smooth ones: its face normal at every vertex
+                    double e1[3], e2[3];
+                    for (int a = 0; a < 3; ++a) {
+                        e1[a] = (double)comp(P[1], a) - comp(P[0], a);
+                        e2[a] = (double)comp(P[2], a) - comp(P[0], a);
+                    }
+                    double cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                                    e1[0] * e2[1] - e1[1] * e2[0]};
+                    double l = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+                    for (int c = 0; c < 3; ++c)
+                        for (int a = 0; a < 3; ++a) nv[3 * c + a] = l > 0.0 ? (float)(cr[a] / l) : 0.0f;
+                }
+                s.nrm.insert(s.nrm.end(), nv, nv + 9);
                 push_tri(s, P[0], P[1], P[2], mat, uv);
                 if (emissive) {
                     aqua_light L{};
@@ -559,6 +577,7 @@ HostScene load_scene_json(const std::string& path, bool allow_missing) {
         throw SceneError(AQUA_ERR_PARSE, path + ": " + e.what());
     }
     decode_textures(tc, allow_missing);
+    if (!any_normals) s.nrm.clear();
     finalize_lights(s);
     return s;
 }

@@ -30,6 +30,8 @@ struct Texture {
 struct HostScene {
     std::vector<float> verts;      // 9 floats per triangle, scene order
     std::vector<float> uvs;        // 6 floats per triangle (zeros when absent)
+    std::vector<float> nrm;        // 9 floats per triangle: vertex normals (scene order), or
+                                   // empty when no mesh of the scene carries normals
     std::vector<int32_t> tri_mat;  // material per triangle
     std::vector<int32_t> tri_light;  // light the triangle belongs to, or -1
     std::vector<aqua_material> mats;

@@ -63,6 +63,21 @@ __device__ __forceinline__ v3 tex_bilinear(const DevScene& S, int ti, float u, f
     return a + (b - a) * ay;
 }
 
+// Shading normal at hit (tri, u, v): the interpolated vertex normal, turned
+// to the side of ng (which faces wo), when wo lies above it; otherwise ng.
+// Flat scenes (no normals) return ng itself.
+__device__ __forceinline__ v3 shading_normal(const DevScene& S, int32_t tri, float u, float v, v3 ng, v3 wo) {
+    if (!S.nrm) return ng;
+    const float4* np = S.nrm + 3 * (size_t)tri;
+    float4 a = ldg_(np), b = ldg_(np + 1), c = ldg_(np + 2);
+    v3 n = f3(a) * (1.0f - u - v) + f3(b) * u + f3(c) * v;
+    float l2 = dot(n, n);
+    if (!(l2 > 0.0f)) return ng;
+    n = n * (1.0f / sqrtf(l2));
+    if (dot(n, ng) < 0.0f) n = -n;
+    return dot(n, wo) > 0.0f ? n : ng;
+}
+
 __device__ __forceinline__ int pick_light(const DevScene& S, float u) {
     int lo = 0, hi = S.n_lights - 1;
     while (lo < hi) {

@@ -280,6 +280,13 @@ AQUA_API aqua_status aqua_scene_export_lights(aqua_ctx* ctx, const aqua_scene* s
 AQUA_API aqua_status aqua_scene_export_texture(aqua_ctx* ctx, const aqua_scene* scene,
                                                int32_t i, int32_t* width, int32_t* height,
                                                uint8_t* rgba);
+/* Vertex normals, 9 floats per triangle in aqua_scene_export_triangles order,
+ * from the meshes' `normals` (a mesh without them contributes its face
+ * normal). *present = 0 when no mesh of the scene has normals: the scene is
+ * then shaded with geometric normals and nrm is left untouched. nrm may be
+ * NULL to query presence. */
+AQUA_API aqua_status aqua_scene_export_normals(aqua_ctx* ctx, const aqua_scene* scene, float* nrm,
+                                               int32_t* present);
 /* Decodes JPEG bytes (the decoder `Image` textures go through; it stands in
  * for the reference's `image` crate, Cargo.toml:13) into 8-bit RGB, row 0 =
  * the top of the image. Pass rgb = NULL to query the size. Works on a

@@ -545,6 +545,22 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
                 break;
             }
             if (dot3(ng, wo) < T(0)) ng = -ng;
+            // Shading normal: the interpolated vertex normal on ng's side when
+            // wo lies above it, else ng (the device's shading_normal).
+            V3<T> ns = ng;
+            if (s->nrm) {
+                const float* nv = s->nrm + 9 * (size_t)h.id;
+                T w0 = T(1) - h.u - h.v;
+                V3<T> n{(T)nv[0] * w0 + (T)nv[3] * h.u + (T)nv[6] * h.v,
+                        (T)nv[1] * w0 + (T)nv[4] * h.u + (T)nv[7] * h.v,
+                        (T)nv[2] * w0 + (T)nv[5] * h.u + (T)nv[8] * h.v};
+                T l2 = dot3(n, n);
+                if (l2 > T(0)) {
+                    n = n * (T(1) / std::sqrt(l2));
+                    if (dot3(n, ng) < T(0)) n = -n;
+                    if (dot3(n, wo) > T(0)) ns = n;
+                }
+            }
             const aqua_material& m = s->mats[s->tri_mat[h.id]];
             V3<T> base{(T)m.base_color[0], (T)m.base_color[1], (T)m.base_color[2]};
             if (m.base_texture >= 0) {
@@ -556,8 +572,8 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
             }
             Mat<T> M = make_mat<T>(base, (T)m.metallic, (T)m.roughness, (T)m.specular);
             V3<T> Tt, Bt;
-            basis(ng, Tt, Bt);
-            V3<T> wol{dot3(wo, Tt), dot3(wo, Bt), dot3(wo, ng)};
+            basis(ns, Tt, Bt);
+            V3<T> wol{dot3(wo, Tt), dot3(wo, Bt), dot3(wo, ns)};
             T u[8];
             for (int k = 0; k < 8; ++k) u[k] = (T)rng.uniform();
             if (s->n_lights > 0 && wol.z > T(0)) {
@@ -574,8 +590,8 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
                     T d2 = dot3(dl, dl);
                     dist = std::sqrt(d2);
                     wi = dl * (T(1) / dist);
-                    T cs = dot3(wi, ng);
-                    if (cs > T(0) && d2 > T(0)) {
+                    T cs = dot3(wi, ns), cg = dot3(wi, ng);
+                    if (cs > T(0) && cg > T(0) && d2 > T(0)) {
                         V3<T> wil{dot3(wi, Tt), dot3(wi, Bt), cs};
                         contrib = thr * eval(M, wol, wil) * le * (cs / (d2 * pmf));
                     }
@@ -593,8 +609,8 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
                     T d2 = dot3(dl, dl);
                     dist = std::sqrt(d2);
                     wi = dl * (T(1) / dist);
-                    T cl = -dot3(wi, nl), cs = dot3(wi, ng);
-                    if (cl > T(0) && cs > T(0) && d2 > T(0)) {
+                    T cl = -dot3(wi, nl), cs = dot3(wi, ns), cg = dot3(wi, ng);
+                    if (cl > T(0) && cs > T(0) && cg > T(0) && d2 > T(0)) {
                         V3<T> wil{dot3(wi, Tt), dot3(wi, Bt), cs};
                         T pl = pmf * d2 / (area * cl);
                         T w = power(pl, pdf(M, wol, wil));
@@ -618,7 +634,8 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
                 if (u[6] >= q) break;
                 thr = thr * (T(1) / q);
             }
-            d = unit(Tt * wil.x + Bt * wil.y + ng * wil.z);
+            d = unit(Tt * wil.x + Bt * wil.y + ns * wil.z);
+            if (s->nrm && !(dot3(d, ng) > T(0))) break;  // below the geometric surface
             o = offset(p, ng);
             pdf_b = pb;
         }

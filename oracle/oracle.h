@@ -49,6 +49,8 @@ typedef struct orc_scene {
     int32_t n_tex;
     aqua_camera cam;
     float env[3];
+    const float* nrm;          /* 9 floats per triangle (vertex normals),
+                                  scene order, or NULL: flat shading      */
 } orc_scene;
 
 /* FP32 traversal of the flattened BVH with the same node order, slab test

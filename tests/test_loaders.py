@@ -47,7 +47,9 @@ def bson_doc(items):
 
 def write_mesh(path, verts, idx, name="m", uvs=None, normals=True):
     items = [("name", name), ("vertices", [[float(c) for c in v] for v in verts])]
-    items.append(("normals", [[0.0, 1.0, 0.0] for _ in verts] if normals else []))
+    if normals is True:
+        normals = [[0.0, 1.0, 0.0] for _ in verts]
+    items.append(("normals", [[float(c) for c in n] for n in normals] if normals else []))
     items.append(("texcoords", [[float(c) for c in t] for t in uvs] if uvs is not None else []))
     items.append(("indices", [[int(c) for c in t] for t in idx]))
     open(path, "wb").write(bson_doc(items))
@@ -116,6 +118,26 @@ def test_image_textures(host_ctx, quad_scene):
     with pytest.raises(aqua.AquaError) as e:
         host_ctx.load_scene(str(p))
     assert e.value.status == aqua.ERR_UNSUPPORTED and "bad.jpg" in str(e.value)
+
+
+def test_vertex_normals(host_ctx, tmp_path):
+    """Mesh `normals` become per-triangle vertex normals; a mesh without them
+    contributes its face normal; a scene with no normals at all is flat."""
+    write_mesh(tmp_path / "a.mesh", [[0, 0, 0], [1, 0, 0], [0, 1, 0]], [[0, 1, 2]],
+               normals=[[0, 0, 1], [0.6, 0, 0.8], [0, 0.6, 0.8]])
+    write_mesh(tmp_path / "b.mesh", [[0, 0, 1], [0, 1, 1], [1, 0, 1]], [[0, 1, 2]], normals=False)
+    p = tmp_path / "s.json"
+    p.write_text(json.dumps(scene_json([("a.mesh", "m"), ("b.mesh", "m")], {"m": principled()})))
+    s = host_ctx.load_scene(str(p))
+    n = s.normals()
+    assert n.shape == (2, 9)
+    np.testing.assert_allclose(n[0], [0, 0, 1, 0.6, 0, 0.8, 0, 0.6, 0.8], atol=1e-7)
+    np.testing.assert_array_equal(n[1], [0, 0, -1] * 3)  # (v1 - v0) x (v2 - v0)
+    s.free()
+    p.write_text(json.dumps(scene_json([("b.mesh", "m")], {"m": principled()})))
+    s = host_ctx.load_scene(str(p))
+    assert s.normals() is None
+    s.free()
 
 
 def test_synthetic_scene_loads(host_ctx, quad_scene):
