@@ -353,10 +353,8 @@ static BatchResult launch_jobs(aqua_ctx* ctx, std::vector<DevJob>& jobs, std::ve
             AQ_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
         }
     }
-    cudaEvent_t e0, e1;
-    AQ_CUDA(cudaEventCreate(&e0));
-    AQ_CUDA(cudaEventCreate(&e1));
-    AQ_CUDA(cudaEventRecord(e0, st));
+    EventPair ev;
+    AQ_CUDA(cudaEventRecord(ev.e[0], st));
     if (g.exec) {
         AQ_CUDA(cudaGraphLaunch(g.exec, st));
     } else {
@@ -367,16 +365,13 @@ static BatchResult launch_jobs(aqua_ctx* ctx, std::vector<DevJob>& jobs, std::ve
                                          g.d_stats);
         AQ_CUDA(cudaGetLastError());
     }
-    AQ_CUDA(cudaEventRecord(e1, st));
+    AQ_CUDA(cudaEventRecord(ev.e[1], st));
     std::vector<unsigned long long> clocks(n + 1);
     unsigned long long hs[4] = {0, 0, 0, 0};
     AQ_CUDA(cudaMemcpyAsync(clocks.data(), g.d_clocks, 8 * (n + 1), cudaMemcpyDeviceToHost, st));
     AQ_CUDA(cudaMemcpyAsync(hs, g.d_stats, 8 * 4, cudaMemcpyDeviceToHost, st));
     AQ_CUDA(cudaStreamSynchronize(st));
-    float ms = 0.0f;
-    AQ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    const float ms = ev.ms();
     BatchResult r;
     r.ms = ms;
     r.paths = hs[0];

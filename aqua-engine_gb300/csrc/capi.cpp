@@ -2,6 +2,7 @@
 // error text, scene upload, and dispatch into the CUDA translation units.
 // No C++ exception crosses this boundary.
 #include <algorithm>
+#include <memory>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -811,23 +812,18 @@ AQUA_API aqua_status aqua_nrc_forward(aqua_ctx* ctx, aqua_nrc* n, const uint16_t
         } else {
             need(((uintptr_t)x & 15) == 0, "x must be 16-byte aligned");
         }
-        cudaEvent_t ev[2] = {nullptr, nullptr};
-        struct EvGuard {
-            cudaEvent_t* e;
-            ~EvGuard() { for (int i = 0; i < 2; ++i) if (e[i]) cudaEventDestroy(e[i]); }
-        } guard_ev{ev};
+        std::unique_ptr<EventPair> ev;
         if (flags & AQUA_NRC_TIMING) {
-            AQ_CUDA(cudaEventCreate(&ev[0]));
-            AQ_CUDA(cudaEventCreate(&ev[1]));
-            AQ_CUDA(cudaEventRecord(ev[0], ctx->stream));
+            ev.reset(new EventPair());
+            AQ_CUDA(cudaEventRecord(ev->e[0], ctx->stream));
         }
         nrc_forward_dev(ctx, n->net, d_x, (int)cnt, d_out);
-        if (flags & AQUA_NRC_TIMING) AQ_CUDA(cudaEventRecord(ev[1], ctx->stream));
+        if (ev) AQ_CUDA(cudaEventRecord(ev->e[1], ctx->stream));
         if (!(flags & AQUA_NRC_DEVICE_PTRS))
             AQ_CUDA(cudaMemcpyAsync(out, d_out, 12 * cnt, cudaMemcpyDeviceToHost, ctx->stream));
         AQ_CUDA(cudaStreamSynchronize(ctx->stream));
         nrc_check_tc(ctx, n->net);
-        if (flags & AQUA_NRC_TIMING) AQ_CUDA(cudaEventElapsedTime(&n->last_ms, ev[0], ev[1]));
+        if (ev) n->last_ms = ev->ms();
     });
 }
 

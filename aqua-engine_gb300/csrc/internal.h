@@ -30,6 +30,31 @@ struct Error : std::runtime_error {
                               std::string(#call) + ": " + cudaGetErrorString(e_));             \
     } while (0)
 
+// A pair of CUDA events for timing one stretch of a stream, destroyed with
+// the object (also when a CUDA call in between throws).
+struct EventPair {
+    cudaEvent_t e[2] = {nullptr, nullptr};
+    EventPair() {
+        cudaError_t r = cudaEventCreate(&e[0]);
+        if (r == cudaSuccess) r = cudaEventCreate(&e[1]);
+        if (r != cudaSuccess) {
+            if (e[0]) cudaEventDestroy(e[0]);
+            AQ_CUDA(r);
+        }
+    }
+    ~EventPair() {
+        for (auto x : e)
+            if (x) cudaEventDestroy(x);
+    }
+    EventPair(const EventPair&) = delete;
+    EventPair& operator=(const EventPair&) = delete;
+    float ms() const {
+        float t = 0.0f;
+        AQ_CUDA(cudaEventElapsedTime(&t, e[0], e[1]));
+        return t;
+    }
+};
+
 // Device buffer owned by a context; size in bytes.
 struct DevBuf {
     void* ptr = nullptr;

@@ -85,21 +85,16 @@ void trace_rays(aqua_ctx* ctx, aqua_scene* sc, const aqua_ray* rays, size_t n, a
     AQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, 0));
     size_t need = (n + 127) / 128;
     int grid = (int)std::min<size_t>(need, (size_t)ctx->num_sms * (size_t)std::max(per_sm, 1));
-    cudaEvent_t e0, e1;
-    AQ_CUDA(cudaEventCreate(&e0));
-    AQ_CUDA(cudaEventCreate(&e1));
-    AQ_CUDA(cudaEventRecord(e0, st));
+    EventPair ev;
+    AQ_CUDA(cudaEventRecord(ev.e[0], st));
     k<<<grid, 128, 0, st>>>(sc->ds, d_rays, n, d_hits, d_stats);
     AQ_CUDA(cudaGetLastError());
-    AQ_CUDA(cudaEventRecord(e1, st));
+    AQ_CUDA(cudaEventRecord(ev.e[1], st));
     if (!dev) AQ_CUDA(cudaMemcpyAsync(out, d_hits, 16 * n, cudaMemcpyDeviceToHost, st));
     unsigned long long hs[2] = {0, 0};
     if (counts) AQ_CUDA(cudaMemcpyAsync(hs, d_stats, 16, cudaMemcpyDeviceToHost, st));
     AQ_CUDA(cudaStreamSynchronize(st));
-    float ms = 0.0f;
-    AQ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    const float ms = ev.ms();
     if (counts) {
         counts->node_visits = hs[0];
         counts->tri_tests = hs[1];
