@@ -8,7 +8,8 @@
 // regeneration), so lanes do not wait for the longest path of their warp.
 // When a pixel has all its samples the lane writes it and, together with
 // the other idle lanes of its warp, takes the next pixels from a global
-// counter in job order. Contributions are summed in the wavefront's order
+// counter; jobs are laid out shortest first (pixels x spp), so small jobs
+// complete early. Contributions are summed in the wavefront's order
 // (emission, then next-event estimation, bounce after bounce, sample after
 // sample), so a job's image matches aqua_render's. The lane that finishes a
 // job's last pixel stamps the device clock, giving per-job latencies.
@@ -419,18 +420,34 @@ void render_batch(aqua_ctx* ctx, const aqua_job* in, size_t n, const aqua_tuning
         d.max_depth = j.max_depth;
         d.rr_depth = 3;
         d.pixels = (uint32_t)j.width * (uint32_t)j.height;
-        d.pixel_begin = total_pixels;
-        if ((uint64_t)total_pixels + d.pixels > 0xFFFFFF00ull)
-            throw Error(AQUA_ERR_INVALID_ARG, "a batch holds at most 2^32 - 256 pixels");
-        total_pixels += d.pixels;
     }
-    BatchResult r = launch_jobs(ctx, jobs, scenes, total_pixels, tune);
+    // Shortest job first: the kernel hands out pixels in the order of the
+    // device job list, so ordering it by work (pixels x spp) lets small jobs
+    // finish early without changing any job's image. rank[i] = position of
+    // input job i.
+    std::vector<size_t> order(n), rank(n);
+    for (size_t i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        return (uint64_t)jobs[a].pixels * (uint64_t)jobs[a].spp < (uint64_t)jobs[b].pixels * (uint64_t)jobs[b].spp;
+    });
+    std::vector<DevJob> sorted(n);
+    for (size_t k = 0; k < n; ++k) {
+        sorted[k] = jobs[order[k]];
+        rank[order[k]] = k;
+        sorted[k].pixel_begin = total_pixels;
+        if ((uint64_t)total_pixels + sorted[k].pixels > 0xFFFFFF00ull)
+            throw Error(AQUA_ERR_INVALID_ARG, "a batch holds at most 2^32 - 256 pixels");
+        total_pixels += sorted[k].pixels;
+    }
+    BatchResult r = launch_jobs(ctx, sorted, scenes, total_pixels, tune);
     if (stats) {
         stats->device_ms = r.ms;
         stats->paths = r.paths;
         if (stats->job_ms)
-            for (size_t i = 0; i < n; ++i)
-                stats->job_ms[i] = r.clocks[1 + i] >= r.clocks[0] ? (double)(r.clocks[1 + i] - r.clocks[0]) * 1e-6 : -1.0;
+            for (size_t i = 0; i < n; ++i) {
+                const unsigned long long c = r.clocks[1 + rank[i]];
+                stats->job_ms[i] = c >= r.clocks[0] ? (double)(c - r.clocks[0]) * 1e-6 : -1.0;
+            }
     }
 }
 

@@ -346,10 +346,11 @@ AQUA_API aqua_status aqua_autotune(aqua_ctx* ctx, aqua_scene* scene,
 
 /* Renders n jobs (views of up to n scenes, uneven resolutions and spp; at
  * most 1024 jobs) in one persistent launch replayed from a captured CUDA
- * graph (tuning->use_graph, on when tuning is NULL). Warps take work units
- * of 32 pixels of one job from a global queue, in job order; each pixel's
- * samples run in one lane, so every job's image equals aqua_render's with
- * one slot per pixel. rgb_out of each job is a device buffer. stats->job_ms,
+ * graph (tuning->use_graph, on when tuning is NULL). Each lane owns one
+ * pixel and runs its samples one path after another; idle lanes take the
+ * next pixels from a global queue on which the jobs are laid out shortest
+ * first (pixels x spp), so small jobs complete early. Every job's image
+ * equals aqua_render's. rgb_out of each job is a device buffer. stats->job_ms,
  * when non-NULL, receives each job's completion time from the start of the
  * launch (device clock). tuning->block_trace = threads per block (64, 128,
  * 256), tuning->blocks_per_sm = persistent blocks per SM (0 = occupancy). */
