@@ -866,9 +866,14 @@ AQUA_API aqua_status aqua_nrc_train_step(aqua_ctx* ctx, aqua_nrc* n, const uint1
             need(((uintptr_t)x & 15) == 0, "x must be 16-byte aligned");
         }
         nrc_train_step_dev(ctx, n->net, d_x, d_t, (int)cnt);
-        double l = 0.0;
-        AQ_CUDA(cudaMemcpyAsync(&l, n->net.loss, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        struct {
+            double loss;
+            uint32_t tc_err, pad;
+        } rb{};  // the loss and, right after it, the tcgen05 error flag
+        AQ_CUDA(cudaMemcpyAsync(&rb, n->net.loss, 16, cudaMemcpyDeviceToHost, ctx->stream));
         AQ_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (rb.tc_err) nrc_check_tc(ctx, n->net);  // resets the flag and throws
+        const double l = rb.loss;
         if (loss) *loss = l / (double)(cnt * kNrcOut);
     });
 }

@@ -97,6 +97,7 @@ struct NrcNet {
     float* ema = nullptr;    // exponential moving average of w (inference weights)
     uint2* frag_inf = nullptr;  // forward fragments of the inference weights
     uint8_t* img_tc = nullptr;  // inference weights in the tcgen05 shared-memory layout
+    uint8_t* img_tc_w = nullptr;  // the trained weights w in that layout (training forward)
     uint32_t* tc_err = nullptr; // set by the tcgen05 kernel when a wait expired
     int forward_tc = 0;         // 1: inference runs on tcgen05 (else mma.sync)
     float ema_decay = 0.0f;  // 0 = inference uses w itself
@@ -195,6 +196,7 @@ struct aqua_ctx {
     std::vector<cudaEvent_t> events;         // pool for stage timing
     aq::DevBuf trace_rays, trace_hits;       // staging for host-pointer traces
     aq::DevBuf persist_film;                 // device film of host-film persistent renders
+    bool nrc_tc_ready = false;               // tcgen05 inference kernel configured on this device
     aq::DevBuf trace_stats;
 };
 
@@ -240,7 +242,8 @@ void nrc_encode_dev(aqua_ctx* ctx, NrcNet& net, const float* raw, int n, uint16_
 // tcgen05 inference (nrc_tc.cu)
 size_t nrc_tc_weight_bytes();
 void nrc_pack_tc(aqua_ctx* ctx, const float* w, void* img);
-void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n, float* out, uint32_t* err);
+void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n, float* out, uint32_t* err,
+                        uint32_t* acts = nullptr);
 // Throws when a tcgen05 launch since the last check gave up waiting (syncs the stream).
 void nrc_check_tc(aqua_ctx* ctx, NrcNet& net);
 

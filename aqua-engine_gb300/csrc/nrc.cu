@@ -356,7 +356,7 @@ void nrc_alloc(aqua_ctx* ctx, NrcNet& net) {
     size_t o_w = take(4 * kNrcParams), o_m = take(4 * kNrcParams), o_v = take(4 * kNrcParams),
            o_g = take(4 * kNrcParams), o_f = take(8 * kFragFwd), o_b = take(8 * kFragBwd), o_l = take(64),
            o_e = take(4 * kNrcParams), o_fi = take(8 * kFragFwd), o_tc = take(nrc_tc_weight_bytes()),
-           o_er = take(4);
+           o_tw = take(nrc_tc_weight_bytes());
     dev_alloc(ctx, net.block, off);
     char* b = (char*)net.block.ptr;
     net.w = (float*)(b + o_w);
@@ -369,7 +369,8 @@ void nrc_alloc(aqua_ctx* ctx, NrcNet& net) {
     net.ema = (float*)(b + o_e);
     net.frag_inf = (uint2*)(b + o_fi);
     net.img_tc = (uint8_t*)(b + o_tc);
-    net.tc_err = (uint32_t*)(b + o_er);
+    net.img_tc_w = (uint8_t*)(b + o_tw);
+    net.tc_err = (uint32_t*)(b + o_l + 8);  // next to the loss: one read-back carries both
     AQ_CUDA(cudaMemsetAsync(net.tc_err, 0, 4, ctx->stream));
 }
 
@@ -399,7 +400,10 @@ void nrc_pack(aqua_ctx* ctx, NrcNet& net) {
     const float* inf = net.ema_decay > 0.0f ? net.ema : net.w;
     k_nrc_pack<<<(kFragFwd + 255) / 256, 256, 0, ctx->stream>>>(inf, net.frag_inf, nullptr);
     AQ_CUDA(cudaGetLastError());
-    if (net.forward_tc) nrc_pack_tc(ctx, inf, net.img_tc);
+    if (net.forward_tc) {
+        nrc_pack_tc(ctx, inf, net.img_tc);
+        nrc_pack_tc(ctx, net.w, net.img_tc_w);
+    }
 }
 
 void nrc_set_weights(aqua_ctx* ctx, NrcNet& net, const float* host_w) {
@@ -455,7 +459,10 @@ void nrc_train_step_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, const flo
     cudaStream_t st = ctx->stream;
     const uint32_t* Xw = reinterpret_cast<const uint32_t*>(X);
     int g = nrc_grid(ctx, n);
-    k_nrc_forward<true><<<g, 128, 0, st>>>(Xw, n, net.frag, net.ty, net.acts);
+    if (net.forward_tc)
+        nrc_forward_tc_dev(ctx, net.img_tc_w, X, n, net.ty, net.tc_err, net.acts);
+    else
+        k_nrc_forward<true><<<g, 128, 0, st>>>(Xw, n, net.frag, net.ty, net.acts);
     AQ_CUDA(cudaMemsetAsync(net.loss, 0, 8, st));
     k_nrc_backward<<<g, 128, 0, st>>>(net.ty, target, n, 1.0f / (float)(n * kNrcOut), net.fragT, net.acts,
                                       net.deltas, net.d6, net.loss);

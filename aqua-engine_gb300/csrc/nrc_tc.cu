@@ -207,10 +207,11 @@ __device__ __forceinline__ uint32_t relu_pack2(uint32_t lo, uint32_t hi) {
 
 // ---------------------------------------------------------------- kernel
 // X (through `xmap`): n rows x 64 bf16; out: n x 3 fp32; err: set to 1 when a
-// wait expired.
+// wait expired. acts (training, may be null): the hidden activations H1..H5
+// as bf16 rows, acts[l][row][64], for the backward pass.
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_nrc_forward_tc(const __grid_constant__ CUtensorMap xmap, int n, const uint4* __restrict__ wimg,
-                     float* __restrict__ out, uint32_t* __restrict__ err) {
+                     float* __restrict__ out, uint32_t* __restrict__ err, uint4* __restrict__ acts) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t bar_in[kTcGroups], bar_mma[kTcGroups];
     __shared__ uint32_t tmem_base_slot;
@@ -255,7 +256,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint32_t tma_par = 0, mma_par = 0;   // parity the work in flight will complete
     bool fail = false, tma_pending = false, mma_pending = false;
 
-    int tile = (int)blockIdx.x * kTcGroups + g;
+    // Tiles interleave across CTAs first, so a small batch still spreads
+    // over many SMs.
+    int tile = (int)blockIdx.x + g * (int)gridDim.x;
     if (gt == 0 && tile < tiles) {
         tma_load_tile(&xmap, sI, mb_in, tile * kTcRows);
         tma_pending = true;
@@ -317,6 +320,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     for (int c = 0; c < 32; ++c) a[c] = relu_pack2(r[2 * c], r[2 * c + 1]);
                     AQ_TC_ST16(tact + lanes + 0u, (a + 0));
                     AQ_TC_ST16(tact + lanes + 16u, (a + 16));
+                    const int grow = tile * kTcRows + row;
+                    if (acts && grow < n) {
+                        uint4* dst = acts + ((size_t)l * (size_t)n + (size_t)grow) * 8;
+#pragma unroll
+                        for (int q4 = 0; q4 < 8; ++q4)
+                            dst[q4] = make_uint4(a[4 * q4], a[4 * q4 + 1], a[4 * q4 + 2], a[4 * q4 + 3]);
+                    }
                     tc_wait_st();
                 } else {
                     uint32_t r[16];
@@ -377,7 +387,8 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
-void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n, float* out, uint32_t* err) {
+void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n, float* out, uint32_t* err,
+                        uint32_t* acts) {
     if (n <= 0) return;
     if (((uintptr_t)X & 15) != 0) throw Error(AQUA_ERR_INVALID_ARG, "x must be 16-byte aligned");
     CUtensorMap map;
@@ -389,11 +400,14 @@ void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n
                                       strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                       CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw Error(AQUA_ERR_CUDA, "cuTensorMapEncodeTiled failed for the query rows");
-    AQ_CUDA(cudaFuncSetAttribute(k_nrc_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
+    if (!ctx->nrc_tc_ready) {  // once per context (one device)
+        AQ_CUDA(cudaFuncSetAttribute(k_nrc_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
+        ctx->nrc_tc_ready = true;
+    }
     const int tiles = (n + kTcRows - 1) / kTcRows;
-    const int grid = std::max(1, std::min((tiles + kTcGroups - 1) / kTcGroups, ctx->num_sms));
+    const int grid = std::max(1, std::min(tiles, ctx->num_sms));
     k_nrc_forward_tc<<<grid, kTcThreads, kTcSmemBytes, ctx->stream>>>(map, n, reinterpret_cast<const uint4*>(img),
-                                                                       out, err);
+                                                                       out, err, reinterpret_cast<uint4*>(acts));
     AQ_CUDA(cudaGetLastError());
 }
 
