@@ -98,6 +98,7 @@ struct NrcNet {
     uint2* frag_inf = nullptr;  // forward fragments of the inference weights
     uint8_t* img_tc = nullptr;  // inference weights in the tcgen05 shared-memory layout
     uint8_t* img_tc_w = nullptr;  // the trained weights w in that layout (training forward)
+    uint8_t* img_tc_bwd = nullptr;  // W6^T, W5^T..W2^T of w in that layout (backward)
     uint32_t* tc_err = nullptr; // set by the tcgen05 kernel when a wait expired
     int forward_tc = 0;         // 1: inference runs on tcgen05 (else mma.sync)
     float ema_decay = 0.0f;  // 0 = inference uses w itself
@@ -197,6 +198,7 @@ struct aqua_ctx {
     aq::DevBuf trace_rays, trace_hits;       // staging for host-pointer traces
     aq::DevBuf persist_film;                 // device film of host-film persistent renders
     bool nrc_tc_ready = false;               // tcgen05 inference kernel configured on this device
+    bool nrc_tc_bwd_ready = false;           // and the tcgen05 backward kernel
     aq::DevBuf trace_stats;
 };
 
@@ -244,6 +246,10 @@ size_t nrc_tc_weight_bytes();
 void nrc_pack_tc(aqua_ctx* ctx, const float* w, void* img);
 void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n, float* out, uint32_t* err,
                         uint32_t* acts = nullptr);
+size_t nrc_tc_bwd_bytes();
+void nrc_pack_bwd_tc(aqua_ctx* ctx, const float* w, void* img);
+void nrc_backward_tc_dev(aqua_ctx* ctx, const void* img, const float* Y, const float* T, int n, float inv_count,
+                         const uint32_t* acts, uint32_t* deltas, uint32_t* d6, double* loss, uint32_t* err);
 // Throws when a tcgen05 launch since the last check gave up waiting (syncs the stream).
 void nrc_check_tc(aqua_ctx* ctx, NrcNet& net);
 

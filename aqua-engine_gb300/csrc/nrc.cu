@@ -356,7 +356,7 @@ void nrc_alloc(aqua_ctx* ctx, NrcNet& net) {
     size_t o_w = take(4 * kNrcParams), o_m = take(4 * kNrcParams), o_v = take(4 * kNrcParams),
            o_g = take(4 * kNrcParams), o_f = take(8 * kFragFwd), o_b = take(8 * kFragBwd), o_l = take(64),
            o_e = take(4 * kNrcParams), o_fi = take(8 * kFragFwd), o_tc = take(nrc_tc_weight_bytes()),
-           o_tw = take(nrc_tc_weight_bytes());
+           o_tw = take(nrc_tc_weight_bytes()), o_tb = take(nrc_tc_bwd_bytes());
     dev_alloc(ctx, net.block, off);
     char* b = (char*)net.block.ptr;
     net.w = (float*)(b + o_w);
@@ -370,6 +370,7 @@ void nrc_alloc(aqua_ctx* ctx, NrcNet& net) {
     net.frag_inf = (uint2*)(b + o_fi);
     net.img_tc = (uint8_t*)(b + o_tc);
     net.img_tc_w = (uint8_t*)(b + o_tw);
+    net.img_tc_bwd = (uint8_t*)(b + o_tb);
     net.tc_err = (uint32_t*)(b + o_l + 8);  // next to the loss: one read-back carries both
     AQ_CUDA(cudaMemsetAsync(net.tc_err, 0, 4, ctx->stream));
 }
@@ -403,6 +404,7 @@ void nrc_pack(aqua_ctx* ctx, NrcNet& net) {
     if (net.forward_tc) {
         nrc_pack_tc(ctx, inf, net.img_tc);
         nrc_pack_tc(ctx, net.w, net.img_tc_w);
+        nrc_pack_bwd_tc(ctx, net.w, net.img_tc_bwd);
     }
 }
 
@@ -464,8 +466,12 @@ void nrc_train_step_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, const flo
     else
         k_nrc_forward<true><<<g, 128, 0, st>>>(Xw, n, net.frag, net.ty, net.acts);
     AQ_CUDA(cudaMemsetAsync(net.loss, 0, 8, st));
-    k_nrc_backward<<<g, 128, 0, st>>>(net.ty, target, n, 1.0f / (float)(n * kNrcOut), net.fragT, net.acts,
-                                      net.deltas, net.d6, net.loss);
+    if (net.forward_tc)
+        nrc_backward_tc_dev(ctx, net.img_tc_bwd, net.ty, target, n, 1.0f / (float)(n * kNrcOut), net.acts,
+                            net.deltas, net.d6, net.loss, net.tc_err);
+    else
+        k_nrc_backward<<<g, 128, 0, st>>>(net.ty, target, n, 1.0f / (float)(n * kNrcOut), net.fragT, net.acts,
+                                          net.deltas, net.d6, net.loss);
     int chunks = (n + kWgChunk - 1) / kWgChunk;
     k_nrc_wgrad<<<dim3(chunks, 6), 128, 0, st>>>(Xw, net.acts, net.deltas, net.d6, n, net.partial);
     net.step++;

@@ -161,6 +161,9 @@ __device__ __forceinline__ bool group_any(int id, bool pred) {
     return r != 0;
 }
 
+// Barrier over one warpgroup (named barrier `id`, 128 threads).
+__device__ __forceinline__ void group_sync(int id) { asm volatile("bar.sync %0, 128;\n" ::"r"(id) : "memory"); }
+
 // One input tile: eight boxes of 8 columns x 128 rows, 16 KB on one mbarrier.
 __device__ __forceinline__ void tma_load_tile(const CUtensorMap* map, uint32_t dst, uint32_t mbar, int row0) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"((uint32_t)kTcTileBytes)
@@ -362,6 +365,190 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
 }
 
+// ---------------------------------------------------------------- backward
+// The training step's backward pass on the same machinery (relative L2 loss
+// of Mueller et al. 2021 with y^2 held constant, as k_nrc_backward). Per
+// 128-row tile: dY (16 columns, 3 used) from Y and the targets becomes the
+// A operand in TMEM; dH5 = dY x W6 (one K = 16 MMA); then for layers 5..1
+// the epilogue masks dH with ReLU'(H) read from the stored activations,
+// rounds to bf16, writes delta_l for the weight gradients and, above layer
+// 1, stores it back to TMEM as the A operand of dH_{l-1} = delta_l x W_l.
+// Weight image (rows = N = 64 inputs, K = outputs): W6^T (K = 16) then
+// W5^T..W2^T (K = 64).
+constexpr int kTcBwdW6Bytes = 64 * 16 * 2;                         // 2 KB
+constexpr int kTcBwdBytes = kTcBwdW6Bytes + 4 * kTcLayerBytes;      // 34 KB
+constexpr int kTcBwdSmemBytes = std::max(kTcBwdBytes + 1024, 120 * 1024);  // one CTA per SM
+constexpr float kTcLossEps = 0.01f;
+
+__global__ void k_nrc_pack_bwd_tc(const float* __restrict__ w, uint8_t* __restrict__ img) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 64 * 16) {  // W6^T: row r = input, k = output (3 used)
+        int r = i / 16, k = i % 16;
+        float x = k < kNrcOut ? w[5 * 4096 + k * 64 + r] : 0.0f;
+        *reinterpret_cast<__nv_bfloat16*>(img + tc_offset(64, r, k)) = __float2bfloat16_rn(x);
+    } else if (i < 64 * 16 + 4 * 4096) {  // W5^T, W4^T, W3^T, W2^T
+        int j = i - 64 * 16, m = j / 4096, r = (j / 64) % 64, k = j % 64;
+        int layer = 4 - m;  // W5 = layer index 4 of the stored weights
+        float x = w[layer * 4096 + k * 64 + r];
+        *reinterpret_cast<__nv_bfloat16*>(img + kTcBwdW6Bytes + m * kTcLayerBytes + tc_offset(64, r, k)) =
+            __float2bfloat16_rn(x);
+    }
+}
+
+__device__ __forceinline__ uint32_t pack2_rn(float lo, float hi) {
+    uint32_t d;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;\n" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
+}
+
+#define AQ_TC_ST8(taddr, r)                                                                            \
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};\n" ::"r"(taddr), \
+                 "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])  \
+                 : "memory")
+
+// Y, T: n x 3 fp32 (outputs, targets); acts: H1..H5 bf16 rows; deltas:
+// delta_1..delta_5 bf16 rows; d6: dY as 16 bf16 per row; loss: += sum of
+// the per-element losses; err: 1 when a wait expired.
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_nrc_backward_tc(const float* __restrict__ Y, const float* __restrict__ T, int n, float inv_count,
+                      const uint4* __restrict__ wimg, const uint4* __restrict__ acts, uint4* __restrict__ deltas,
+                      uint4* __restrict__ d6, double* __restrict__ loss, uint32_t* __restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t bar_mma[kTcGroups];
+    __shared__ uint32_t tmem_base_slot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int g = warp >> 2, q = warp & 3, gt = tid & 127;
+    const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    uint8_t* sbase = smem_raw + (base - smem_u32(smem_raw));
+    for (int i = tid; i < kTcBwdBytes / 16; i += kTcThreads) reinterpret_cast<uint4*>(sbase)[i] = wimg[i];
+    if (tid < kTcGroups)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar_mma[tid])) : "memory");
+    if (tid == 0) asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         smem_u32(&tmem_base_slot)),
+                     "r"(kTcTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base_slot + (uint32_t)g * kTcGroupCols;
+    const uint32_t tact = tmem + kTcActCol;
+    const uint32_t lanes = (uint32_t)(q * 32) << 16;
+    const uint32_t mb = smem_u32(&bar_mma[g]);
+    const int bar_id = 1 + g;
+    const int tiles = (n + kTcRows - 1) / kTcRows;
+    const int row = q * 32 + lane;
+    uint32_t ph = 0, mma_par = 0;
+    bool fail = false, pending = false;
+    float lsum = 0.0f;
+    for (int tile = (int)blockIdx.x + g * (int)gridDim.x; tile < tiles; tile += (int)gridDim.x * kTcGroups) {
+        const int grow = tile * kTcRows + row;
+        const bool valid = grow < n;
+        // dY of this row (columns 0..2), packed as 16 bf16.
+        float gy[3] = {0.0f, 0.0f, 0.0f};
+        if (valid) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float y = Y[(size_t)grow * 3 + c], t = T[(size_t)grow * 3 + c];
+                float den = y * y + kTcLossEps, d = y - t;
+                lsum += d * d / den;
+                gy[c] = 2.0f * d / den * inv_count;
+            }
+        }
+        uint32_t a6[8] = {pack2_rn(gy[0], gy[1]), pack2_rn(gy[2], 0.0f), 0u, 0u, 0u, 0u, 0u, 0u};
+        if (valid) {
+            d6[(size_t)grow * 2] = make_uint4(a6[0], a6[1], 0u, 0u);
+            d6[(size_t)grow * 2 + 1] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        AQ_TC_ST8(tact + lanes, a6);
+        asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+        tc_fence_before();
+        group_sync(bar_id);  // dY is in TMEM before the first MMA
+        for (int l = 4; l >= 0; --l) {  // this MMA gives dH of hidden layer l + 1
+            if (gt == 0) {
+                tc_fence_after();
+                const uint32_t idesc = tc_idesc(kTcRows, 64);
+                if (l == 4) {
+                    tc_mma_ts(tmem, tact, tc_desc(base, 64 * 16), idesc, 0u);
+                } else {
+                    const uint32_t b0 = base + kTcBwdW6Bytes + (uint32_t)(3 - l) * kTcLayerBytes;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        tc_mma_ts(tmem, tact + (uint32_t)k * 8u, tc_desc(b0 + (uint32_t)k * 2u * (64 * 16), 64 * 16),
+                                  idesc, k > 0 ? 1u : 0u);
+                }
+                tc_commit(mb);
+                pending = true;
+                mma_par = ph;
+            }
+            bool ok = mbar_wait(mb, ph);
+            ph ^= 1u;
+            ok = __all_sync(0xffffffffu, ok);
+            if (gt == 0 && ok) pending = false;
+            tc_fence_after();
+            if (ok) {
+                uint32_t r[64], a[32];
+                AQ_TC_LD16(tmem + lanes + 0u, (r + 0));
+                AQ_TC_LD16(tmem + lanes + 16u, (r + 16));
+                AQ_TC_LD16(tmem + lanes + 32u, (r + 32));
+                AQ_TC_LD16(tmem + lanes + 48u, (r + 48));
+                tc_wait_ld();
+                // ReLU'(Z) from the stored activation H = ReLU(Z) in bf16.
+                uint4 h[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    h[j] = valid ? acts[((size_t)l * (size_t)n + (size_t)grow) * 8 + (size_t)j] : make_uint4(0, 0, 0, 0);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const uint32_t hw[4] = {h[j].x, h[j].y, h[j].z, h[j].w};
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int c = 4 * j + e;  // bf16 pair (2c, 2c + 1)
+                        float lo = __uint_as_float(r[2 * c]), hi = __uint_as_float(r[2 * c + 1]);
+                        if (!(__uint_as_float(hw[e] << 16) > 0.0f)) lo = 0.0f;
+                        if (!(__uint_as_float(hw[e] & 0xffff0000u) > 0.0f)) hi = 0.0f;
+                        a[c] = pack2_rn(lo, hi);
+                    }
+                }
+                if (valid) {
+                    uint4* dst = deltas + ((size_t)l * (size_t)n + (size_t)grow) * 8;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) dst[j] = make_uint4(a[4 * j], a[4 * j + 1], a[4 * j + 2], a[4 * j + 3]);
+                }
+                if (l > 0) {
+                    AQ_TC_ST16(tact + lanes + 0u, (a + 0));
+                    AQ_TC_ST16(tact + lanes + 16u, (a + 16));
+                    tc_wait_st();
+                }
+            }
+            tc_fence_before();
+            if (group_any(bar_id, !ok)) {
+                fail = true;
+                break;
+            }
+        }
+        if (fail) break;
+    }
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+    if (lane == 0 && lsum != 0.0f) atomicAdd(loss, (double)lsum);
+    if (fail && gt == 0) {
+        atomicExch(err, 1u);
+        if (pending) mbar_wait(mb, mma_par);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem_base_slot),
+                     "r"(kTcTmemCols)
+                     : "memory");
+    }
+}
+
 // ---------------------------------------------------------------- host side
 size_t nrc_tc_weight_bytes() { return (size_t)kTcWeightBytes; }
 
@@ -408,6 +595,31 @@ void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n
     const int grid = std::max(1, std::min(tiles, ctx->num_sms));
     k_nrc_forward_tc<<<grid, kTcThreads, kTcSmemBytes, ctx->stream>>>(map, n, reinterpret_cast<const uint4*>(img),
                                                                        out, err, reinterpret_cast<uint4*>(acts));
+    AQ_CUDA(cudaGetLastError());
+}
+
+
+size_t nrc_tc_bwd_bytes() { return (size_t)kTcBwdBytes; }
+
+void nrc_pack_bwd_tc(aqua_ctx* ctx, const float* w, void* img) {
+    int total = 64 * 16 + 4 * 4096;
+    k_nrc_pack_bwd_tc<<<(total + 255) / 256, 256, 0, ctx->stream>>>(w, (uint8_t*)img);
+    AQ_CUDA(cudaGetLastError());
+}
+
+void nrc_backward_tc_dev(aqua_ctx* ctx, const void* img, const float* Y, const float* T, int n, float inv_count,
+                         const uint32_t* acts, uint32_t* deltas, uint32_t* d6, double* loss, uint32_t* err) {
+    if (n <= 0) return;
+    if (!ctx->nrc_tc_bwd_ready) {
+        AQ_CUDA(cudaFuncSetAttribute(k_nrc_backward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     kTcBwdSmemBytes));
+        ctx->nrc_tc_bwd_ready = true;
+    }
+    const int tiles = (n + kTcRows - 1) / kTcRows;
+    const int grid = std::max(1, std::min(tiles, ctx->num_sms));
+    k_nrc_backward_tc<<<grid, kTcThreads, kTcBwdSmemBytes, ctx->stream>>>(
+        Y, T, n, inv_count, reinterpret_cast<const uint4*>(img), reinterpret_cast<const uint4*>(acts),
+        reinterpret_cast<uint4*>(deltas), reinterpret_cast<uint4*>(d6), loss, err);
     AQ_CUDA(cudaGetLastError());
 }
 
