@@ -168,9 +168,9 @@ NRC_WORKLOAD = {"workload": "interior-320x180-depth8-cache-vs-plain",
                 "width": 320, "height": 180, "max_depth": 8, "rr_depth": 3, "reference_spp": 65536,
                 "frame_spp": 32, "train_records_per_frame": 65536, "batch": 16384, "learning_rate": 1e-2,
                 "query_vertex": 4, "burn_in_frames": 8, "target_relmse": 1e-3, "ema_decay": 0.0,
-                "note": "config 4 scaled to 320x180: 32 spp per frame keeps 1.8M paths and 65,536 training "
-                        "records per frame, as at 1080p and 1 spp; queried at vertex 4 (config: vertex >= 2; "
-                        "vertex 2 / 3 / 5 measured 4.4x / 1.8x / 0.82x of the plain time)"}
+                "note": "the 1080p, 1-spp-per-frame cache workload scaled to 320x180: 32 spp per frame keeps "
+                        "1.8M paths and 65,536 training records per frame; queried at vertex 4 (allowed: vertex "
+                        ">= 2; vertex 2 / 3 / 5 measured 4.4x / 1.8x / 0.82x of the plain time)"}
 
 
 _NRC_REF = {}
