@@ -352,8 +352,9 @@ class Scene:
         return a
 
     def bvh(self):
+        """(nodes, tri_order): the four-wide BVH, 32 floats per node."""
         inf = self.info()
-        nodes = np.zeros((inf.num_bvh_nodes, 16), np.float32)
+        nodes = np.zeros((inf.num_bvh_nodes, 32), np.float32)
         order = np.zeros(inf.num_triangles, np.int32)
         self.ctx._check(self.ctx.lib.aqua_scene_export_bvh(self.ctx.handle, self.handle, _ptr(nodes), _ptr(order)))
         return nodes, order

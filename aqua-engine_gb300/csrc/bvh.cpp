@@ -7,6 +7,7 @@
 #include <cfloat>
 #include <cstring>
 #include <future>
+#include <limits>
 #include <thread>
 
 namespace aq {
@@ -212,58 +213,98 @@ FlatBvh build_bvh(const float* verts, size_t num_tris) {
         tree.push_back(b);
     }
 
-    // Depth-first numbering of inner nodes; leaves in the same order.
-    std::vector<int> flat_id(tree.size(), -1);
-    std::vector<int> order;
-    order.reserve(tree.size());
+    // Collapse into wide nodes, numbered depth first: wide[k] lists the
+    // binary nodes that become node k's children, in spatial (left to right)
+    // order; an inner child of largest surface area is replaced by its two
+    // children while fewer than kBvhWidth are held (ties: the leftmost).
+    struct Wide {
+        int ch[kBvhWidth];
+        int n;
+    };
+    std::vector<Wide> wide;
+    std::vector<int> wid(tree.size(), -1);
     {
         std::vector<int> st{0};
         while (!st.empty()) {
-            int i = st.back();
+            int b = st.back();
             st.pop_back();
-            if (tree[(size_t)i].leaf()) continue;
-            flat_id[(size_t)i] = (int)order.size();
-            order.push_back(i);
-            st.push_back(tree[(size_t)i].right);
-            st.push_back(tree[(size_t)i].left);
+            Wide w;
+            w.n = 2;
+            w.ch[0] = tree[(size_t)b].left;
+            w.ch[1] = tree[(size_t)b].right;
+            while (w.n < kBvhWidth) {
+                int pick = -1;
+                double best = -1.0;
+                for (int k = 0; k < w.n; ++k) {
+                    const BNode& c = tree[(size_t)w.ch[k]];
+                    if (c.leaf()) continue;
+                    double a = c.box.area();
+                    if (a > best) { best = a; pick = k; }
+                }
+                if (pick < 0) break;
+                int l = tree[(size_t)w.ch[pick]].left, r = tree[(size_t)w.ch[pick]].right;
+                for (int k = w.n; k > pick + 1; --k) w.ch[k] = w.ch[k - 1];
+                w.ch[pick] = l;
+                w.ch[pick + 1] = r;
+                ++w.n;
+            }
+            wid[(size_t)b] = (int)wide.size();
+            wide.push_back(w);
+            for (int k = w.n - 1; k >= 0; --k)
+                if (!tree[(size_t)w.ch[k]].leaf()) st.push_back(w.ch[k]);
         }
     }
-    out.nodes.assign(16 * order.size(), 0.0f);
+
+    const float inf = std::numeric_limits<float>::infinity();
+    out.nodes.assign((size_t)kBvhNodeFloats * wide.size(), 0.0f);
     out.tri_order.reserve(num_tris);
     int max_leaf = 0;
-    // Depth of every inner node (root = 1).
-    std::vector<int> depth(tree.size(), 0);
+    // Depth of every wide node (root = 1) and the stack entries a ray holds
+    // when it arrives there (the other hit children pushed on the way).
+    std::vector<int> depth(wide.size(), 0), need(wide.size(), 0);
     depth[0] = 1;
-    int max_depth = 1;
-    for (size_t k = 0; k < order.size(); ++k) {
-        const BNode& nd = tree[(size_t)order[k]];
-        float* w = &out.nodes[16 * k];
-        int32_t link[4];
-        const BNode* ch[2] = {&tree[(size_t)nd.left], &tree[(size_t)nd.right]};
-        for (int c = 0; c < 2; ++c) {
-            const BNode& cn = *ch[c];
-            int ci = c == 0 ? nd.left : nd.right;
-            w[4 * c + 0] = cn.box.lo[0];
-            w[4 * c + 1] = cn.box.hi[0];
-            w[4 * c + 2] = cn.box.lo[1];
-            w[4 * c + 3] = cn.box.hi[1];
-            w[8 + 2 * c + 0] = cn.box.lo[2];
-            w[8 + 2 * c + 1] = cn.box.hi[2];
+    int max_depth = 1, max_stack = 0;
+    for (size_t k = 0; k < wide.size(); ++k) {
+        const Wide& wn = wide[k];
+        float* w = &out.nodes[(size_t)kBvhNodeFloats * k];
+        int32_t link[kBvhWidth], count[kBvhWidth];
+        const int pushes = need[k] + wn.n - 1;
+        max_stack = std::max(max_stack, pushes);
+        for (int c = 0; c < kBvhWidth; ++c) {
+            if (c >= wn.n) {
+                for (int a = 0; a < 6; ++a) w[4 * a + c] = inf;
+                link[c] = ~0;
+                count[c] = 0;
+                continue;
+            }
+            const BNode& cn = tree[(size_t)wn.ch[c]];
+            for (int a = 0; a < 3; ++a) {
+                w[8 * a + c] = cn.box.lo[a];
+                w[8 * a + 4 + c] = cn.box.hi[a];
+            }
             if (cn.leaf()) {
                 int first = (int)out.tri_order.size();
                 for (int i = 0; i < cn.count; ++i) out.tri_order.push_back(refs[(size_t)(cn.first + i)]);
                 link[c] = ~((first << 3) | cn.count);
-                link[2 + c] = cn.count;
+                count[c] = cn.count;
                 max_leaf = std::max(max_leaf, cn.count);
             } else {
-                link[c] = flat_id[(size_t)ci];
-                link[2 + c] = 0;
-                depth[(size_t)ci] = depth[(size_t)order[k]] + 1;
+                int ci = wid[(size_t)wn.ch[c]];
+                link[c] = ci;
+                count[c] = 0;
+                depth[(size_t)ci] = depth[k] + 1;
+                need[(size_t)ci] = pushes;
                 max_depth = std::max(max_depth, depth[(size_t)ci]);
             }
         }
-        memcpy(&w[12], link, sizeof(link));
+        memcpy(&w[24], link, sizeof(link));
+        memcpy(&w[28], count, sizeof(count));
     }
+    for (int a = 0; a < 3; ++a) {
+        out.lo[a] = tree[0].box.lo[a];
+        out.hi[a] = tree[0].box.hi[a];
+    }
+    out.max_stack = max_stack;
     out.depth = max_depth;
     out.max_leaf = max_leaf;
     return out;

@@ -3,19 +3,24 @@
 // The reference's builder was never written (src/lib.rs is empty; the
 // `ordered-float` dependency at Cargo.toml:19 hints at a sorted SAH). This
 // builder bins centroids (32 bins, 3 axes; Wald 2007, "On fast Construction of
-// SAH-based Bounding Volume Hierarchies") and writes a two-wide node array the
-// traversal kernels read with 128-bit loads.
+// SAH-based Bounding Volume Hierarchies") into a binary tree, then collapses
+// it into a four-wide tree: every wide node takes a binary node's two
+// children and keeps opening the inner child of largest surface area until it
+// holds four (the collapse of Wald, Benthin and Boulos 2008, "Getting Rid of
+// Packets"). One node fetch then tests four boxes, halving the chain of
+// dependent node loads a ray walks.
 //
-// Device node layout: 64 bytes = four 16-byte words, both children's boxes in
-// the parent so one node fetch tests two boxes.
-//   w0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
-//   w1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
-//   w2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
-//   w3 = (child0, child1, count0, count1) as int32
+// Device node layout: 128 bytes = eight 16-byte words, the four children's
+// boxes side by side (slot k in component k of each word):
+//   w0 = lo.x   w1 = hi.x   w2 = lo.y   w3 = hi.y   w4 = lo.z   w5 = hi.z
+//   w6 = (child0, child1, child2, child3) as int32
+//   w7 = (count0, count1, count2, count3) as int32 (not read by the kernels)
 // child >= 0: index of an inner node. child < 0: leaf; ~child = first << 3 |
 // count, the leaf's triangles being tri_order[first .. first + count) (count
-// <= kBvhMaxLeaf <= 7; the count is repeated in count0/count1). Node 0 is the
-// root.
+// <= kBvhMaxLeaf <= 7). A node with fewer than four children fills the rest
+// with empty slots: box lo = hi = +inf on every axis (missed by every ray) and
+// child = ~0, a leaf of no triangles. Node 0 is the root; nodes are numbered
+// depth first, children in slot order.
 //
 // Triangle layout (leaf order): three 16-byte words per triangle,
 //   t0 = (v0.xyz, scene index as int bits)
@@ -30,14 +35,18 @@
 namespace aq {
 
 constexpr int kBvhMaxLeaf = 4;
-constexpr int kBvhMaxDepth = 64;  // traversal stack bound
+constexpr int kBvhWidth = 4;
+constexpr int kBvhNodeFloats = 32;   // 128-byte node
+constexpr int kBvhStackSize = 96;    // traversal stack entries per ray
 
 struct FlatBvh {
-    std::vector<float> nodes;        // 16 floats per node
+    std::vector<float> nodes;        // kBvhNodeFloats per node
     std::vector<int32_t> tri_order;  // leaf order -> scene triangle index
-    int depth = 0;
+    int depth = 0;                   // wide nodes on the longest root-leaf path
     int max_leaf = 0;
-    int num_nodes() const { return (int)(nodes.size() / 16); }
+    int max_stack = 0;               // most stack entries a traversal can hold
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // scene bounds
+    int num_nodes() const { return (int)(nodes.size() / kBvhNodeFloats); }
 };
 
 // verts: 9 floats per triangle.

@@ -81,11 +81,11 @@ void scene_build_device(aqua_ctx* ctx, aqua_scene* s) {
     if (h.lights.size() > 65534) throw Error(AQUA_ERR_UNSUPPORTED, "more than 65534 lights");
     if (nt >= (1u << 28)) throw Error(AQUA_ERR_UNSUPPORTED, "more than 2^28 triangles");
     s->bvh = build_bvh(h.verts.data(), nt);
-    if (s->bvh.depth > kBvhMaxDepth) throw Error(AQUA_ERR_UNSUPPORTED, "BVH deeper than the traversal stack");
+    if (s->bvh.max_stack >= kBvhStackSize) throw Error(AQUA_ERR_UNSUPPORTED, "BVH deeper than the traversal stack");
     size_t nn = (size_t)s->bvh.num_nodes();
     size_t texels = 0;
     for (auto& t : h.textures) texels += (size_t)t.w * (size_t)t.h;
-    size_t o_nodes = 0, o_tris = align256(o_nodes + 64 * nn), o_uvs = align256(o_tris + 48 * nt),
+    size_t o_nodes = 0, o_tris = align256(o_nodes + sizeof(float) * kBvhNodeFloats * nn), o_uvs = align256(o_tris + 48 * nt),
            o_mats = align256(o_uvs + 24 * nt), o_lights = align256(o_mats + 32 * h.mats.size()),
            o_texs = align256(o_lights + 64 * h.lights.size()),
            o_texels = align256(o_texs + 16 * h.textures.size()), o_nrm = align256(o_texels + 4 * texels),
@@ -101,7 +101,7 @@ void scene_build_device(aqua_ctx* ctx, aqua_scene* s) {
     }
     char* p = (char*)s->pinned;
     memset(p, 0, total);
-    memcpy(p + o_nodes, s->bvh.nodes.data(), 64 * nn);
+    memcpy(p + o_nodes, s->bvh.nodes.data(), sizeof(float) * kBvhNodeFloats * nn);
     float* tw = (float*)(p + o_tris);
     float* uw = (float*)(p + o_uvs);
     float* nw = h.nrm.empty() ? nullptr : (float*)(p + o_nrm);

@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include "aq_math.h"
+#include "bvh.h"
 
 namespace aq {
 
@@ -31,7 +32,7 @@ struct DevCamera {
     int32_t width, height;
 };
 struct DevScene {
-    const float4* __restrict__ nodes;  // 4 words per node (bvh.h)
+    const float4* __restrict__ nodes;  // 8 words per four-wide node (bvh.h)
     const float4* __restrict__ tris;   // 3 words per triangle, leaf order
     const float2* __restrict__ uvs;    // 3 per triangle, leaf order
     const DevMaterial* __restrict__ mats;
@@ -57,13 +58,56 @@ struct TraceResult {
 template <class T>
 __device__ __forceinline__ T ldg_(const T* p) { return __ldg(p); }
 
-constexpr int kStackSize = 64;  // >= BVH depth (builder bound kBvhMaxDepth)
+constexpr int kStackSize = kBvhStackSize;  // the builder checks its trees fit
+constexpr int32_t kTraversalDone = (int32_t)0x80000000;
 
-// Stack-based traversal of the two-wide BVH (near child first, far child
-// pushed). ANY: stop at the first hit in (tmin, tmax). Otherwise the result is
-// the lexicographic minimum (t, scene index) over all triangles hit: boxes are
-// tested conservatively (slab_entry), a child is skipped only when its entry
-// distance exceeds the best t, so the answer does not depend on visit order.
+// One compare-exchange of the child-ordering network: (ta, ca) gets the
+// nearer entry, ties keep their order.
+__device__ __forceinline__ void order2(float& ta, int32_t& ca, float& tb, int32_t& cb) {
+    const bool sw = tb < ta;
+    const float t = sw ? tb : ta;
+    const int32_t c = sw ? cb : ca;
+    tb = sw ? ta : tb;
+    cb = sw ? ca : cb;
+    ta = t;
+    ca = c;
+}
+
+// Visits four-wide node `node`: tests its four child boxes (slab_entry, far
+// limit tfar), orders the hit children by entry distance (a five-comparator
+// sorting network), pushes all but the nearest, farthest first, and returns
+// the nearest. With no box hit it returns the top of the stack, or
+// kTraversalDone when the stack is empty. Seven 128-bit loads per node (the
+// counts word is not read).
+__device__ __forceinline__ int32_t visit_wide(const DevScene& S, int32_t node, const RayPre& rp, float tfar,
+                                              int32_t* stack, int& sp) {
+    const float4* np = S.nodes + 8 * (size_t)node;
+    const float4 lx = ldg_(np), hx = ldg_(np + 1), ly = ldg_(np + 2), hy = ldg_(np + 3);
+    const float4 lz = ldg_(np + 4), hz = ldg_(np + 5);
+    const int4 ch = ldg_(reinterpret_cast<const int4*>(np + 6));
+    float t0 = slab_entry(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, rp, tfar);
+    float t1 = slab_entry(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, rp, tfar);
+    float t2 = slab_entry(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, rp, tfar);
+    float t3 = slab_entry(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, rp, tfar);
+    int32_t c0 = ch.x, c1 = ch.y, c2 = ch.z, c3 = ch.w;
+    order2(t0, c0, t1, c1);
+    order2(t2, c2, t3, c3);
+    order2(t0, c0, t2, c2);
+    order2(t1, c1, t3, c3);
+    order2(t1, c1, t2, c2);
+    if (t3 != INFINITY) stack[sp++] = c3;
+    if (t2 != INFINITY) stack[sp++] = c2;
+    if (t1 != INFINITY) stack[sp++] = c1;
+    if (t0 != INFINITY) return c0;
+    return sp > 0 ? stack[--sp] : kTraversalDone;
+}
+
+// Stack-based traversal of the four-wide BVH (nearest child first, the other
+// hit children pushed farthest first). ANY: stop at the first hit in (tmin,
+// tmax). Otherwise the result is the lexicographic minimum (t, scene index)
+// over all triangles hit: boxes are tested conservatively (slab_entry), a
+// child is skipped only when its entry distance exceeds the best t, so the
+// answer does not depend on visit order.
 // COUNT: add inner-node visits and triangle tests to the counters.
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ TraceResult traverse(const DevScene& S, v3 o, v3 d, float tmin, float tmax,
@@ -81,27 +125,10 @@ __device__ __forceinline__ TraceResult traverse(const DevScene& S, v3 o, v3 d, f
     int32_t node = 0;
     while (true) {
         while (node >= 0) {
-            const float4* np = S.nodes + 4 * (size_t)node;
-            float4 w0 = ldg_(np), w1 = ldg_(np + 1), w2 = ldg_(np + 2);
-            int4 w3 = ldg_(reinterpret_cast<const int4*>(np + 3));
             if (COUNT) ++n_nodes;
-            float t0 = slab_entry(w0.x, w0.y, w0.z, w0.w, w2.x, w2.y, rp, r.t);
-            float t1 = slab_entry(w1.x, w1.y, w1.z, w1.w, w2.z, w2.w, rp, r.t);
-            bool h0 = t0 != INFINITY, h1 = t1 != INFINITY;
-            if (h0 && h1) {
-                bool swap = t1 < t0;
-                int32_t nearc = swap ? w3.y : w3.x, farc = swap ? w3.x : w3.y;
-                stack[sp++] = farc;
-                node = nearc;
-            } else if (h0) {
-                node = w3.x;
-            } else if (h1) {
-                node = w3.y;
-            } else {
-                if (sp == 0) return r;
-                node = stack[--sp];
-            }
+            node = visit_wide(S, node, rp, r.t, stack, sp);
         }
+        if (node == kTraversalDone) return r;
         // Leaf.
         int32_t code = ~node;
         int32_t first = code >> 3, cnt = code & 7;
@@ -133,8 +160,6 @@ __device__ __forceinline__ TraceResult traverse(const DevScene& S, v3 o, v3 d, f
 // and triangle tests are those of traverse(), so the result (the minimum
 // (t, scene index) over all triangles hit, or any hit) is identical; only
 // the order of visits, and thus the work counts, differ.
-constexpr int32_t kTraversalDone = (int32_t)0x80000000;
-
 template <bool ANY>
 __device__ __forceinline__ TraceResult traverse_fast(const DevScene& S, v3 o, v3 d, float tmin, float tmax) {
     RayPre rp;
@@ -150,23 +175,7 @@ __device__ __forceinline__ TraceResult traverse_fast(const DevScene& S, v3 o, v3
     int32_t node = 0, leaf = 0;
     while (true) {
         while (node >= 0) {
-            const float4* np = S.nodes + 4 * (size_t)node;
-            float4 w0 = ldg_(np), w1 = ldg_(np + 1), w2 = ldg_(np + 2);
-            int4 w3 = ldg_(reinterpret_cast<const int4*>(np + 3));
-            float t0 = slab_entry(w0.x, w0.y, w0.z, w0.w, w2.x, w2.y, rp, r.t);
-            float t1 = slab_entry(w1.x, w1.y, w1.z, w1.w, w2.z, w2.w, rp, r.t);
-            bool h0 = t0 != INFINITY, h1 = t1 != INFINITY;
-            if (h0 && h1) {
-                bool swap = t1 < t0;
-                stack[sp++] = swap ? w3.x : w3.y;
-                node = swap ? w3.y : w3.x;
-            } else if (h0) {
-                node = w3.x;
-            } else if (h1) {
-                node = w3.y;
-            } else {
-                node = sp > 0 ? stack[--sp] : kTraversalDone;
-            }
+            node = visit_wide(S, node, rp, r.t, stack, sp);
             if (node < 0 && node != kTraversalDone && leaf == 0) {
                 leaf = node;
                 node = sp > 0 ? stack[--sp] : kTraversalDone;
@@ -258,23 +267,7 @@ __device__ __forceinline__ void traverse_queue(const DevScene& S, uint32_t n, ui
         if (!have) continue;
         // One round of traverse_fast.
         while (node >= 0) {
-            const float4* np = S.nodes + 4 * (size_t)node;
-            float4 w0 = ldg_(np), w1 = ldg_(np + 1), w2 = ldg_(np + 2);
-            int4 w3 = ldg_(reinterpret_cast<const int4*>(np + 3));
-            float t0 = slab_entry(w0.x, w0.y, w0.z, w0.w, w2.x, w2.y, rp, r.t);
-            float t1 = slab_entry(w1.x, w1.y, w1.z, w1.w, w2.z, w2.w, rp, r.t);
-            bool h0 = t0 != INFINITY, h1 = t1 != INFINITY;
-            if (h0 && h1) {
-                bool swap = t1 < t0;
-                stack[sp++] = swap ? w3.x : w3.y;
-                node = swap ? w3.y : w3.x;
-            } else if (h0) {
-                node = w3.x;
-            } else if (h1) {
-                node = w3.y;
-            } else {
-                node = sp > 0 ? stack[--sp] : kTraversalDone;
-            }
+            node = visit_wide(S, node, rp, r.t, stack, sp);
             if (node < 0 && node != kTraversalDone && leaf == 0) {
                 leaf = node;
                 node = sp > 0 ? stack[--sp] : kTraversalDone;

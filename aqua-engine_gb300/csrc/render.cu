@@ -944,12 +944,9 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
 
     // Positions are encoded relative to the scene's bounding box.
     {
-        const float* n0 = sc->bvh.nodes.data();
-        float lo[3] = {std::min(n0[0], n0[4]), std::min(n0[2], n0[6]), std::min(n0[8], n0[10])};
-        float hi[3] = {std::max(n0[1], n0[5]), std::max(n0[3], n0[7]), std::max(n0[9], n0[11])};
         for (int k = 0; k < 3; ++k) {
-            net.bmin[k] = lo[k];
-            net.bext[k] = std::max(hi[k] - lo[k], 1e-6f);
+            net.bmin[k] = sc->bvh.lo[k];
+            net.bext[k] = std::max(sc->bvh.hi[k] - sc->bvh.lo[k], 1e-6f);
         }
     }
     const bool visualize = cfg.visualize_cache != 0;

@@ -333,6 +333,7 @@ NRC_INFER_WORKLOAD = {"workload": "nrc-inference-16777216-rows", "rows": 1 << 24
                       "network": "64 -> 5 x 64 (ReLU) -> 3, bf16 operands, fp32 accumulation",
                       "inputs": "encoded from uniform random vertex features (positions in the unit box, "
                                 "unit directions and normals, albedos), seed 21"}
+NODE_BYTES = 112  # a four-wide node visit reads seven 16-byte words (its counts word is not read)
 NRC_FLOP_PER_ROW = 2 * (5 * 64 * 64 + 3 * 64)  # 41,344 useful multiply-adds x 2
 NRC_BYTES_PER_ROW = 128 + 12                   # bf16 input row + fp32 output
 
@@ -507,7 +508,7 @@ def run_gpu(args, world, rank, local, pg):
     trace_ms = sum(s.trace_ms for s in steps)
     launches = sum(s.trace_launches for s in steps)
     ext = cst.ext_rays
-    bytes_step = cst.node_visits * 64 + cst.tri_tests * 48 + ext * (32 + 16)
+    bytes_step = cst.node_visits * NODE_BYTES + cst.tri_tests * 48 + ext * (32 + 16)
     bytes_per_launch = bytes_step / max(cst.trace_launches, 1)
     avg_launch_s = trace_ms * 1e-3 / max(launches, 1)
     achieved = bytes_per_launch / avg_launch_s / 1e9
@@ -515,8 +516,9 @@ def run_gpu(args, world, rank, local, pg):
                 "traffic": args.traffic_per_launch, "peak_source": peak_src,
                 "kernel": "k_trace_ext (closest-hit BVH traversal)",
                 "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6,
-                "note": "algorithmic bytes = node visits x 64 B + triangle tests x 48 B + 48 B per ray; "
-                        "the Cornell BVH (19 nodes) is cache-resident, so DRAM traffic is far below this"}
+                "note": f"algorithmic bytes = node visits x {NODE_BYTES} B (four-wide node: six box words and the "
+                        "child links) + triangle tests x 48 B + 48 B per ray; the Cornell BVH (8 nodes) is "
+                        "cache-resident, so DRAM traffic is far below this"}
 
     # End to end through the C ABI with host buffers: scene upload + render
     # + film download every step.

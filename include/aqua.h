@@ -173,8 +173,8 @@ enum {
 typedef struct aqua_scene_info {
     int32_t width, height;
     int32_t num_triangles, num_materials, num_lights, num_textures;
-    int32_t num_meshes, num_bvh_nodes;
-    int32_t bvh_depth, max_leaf_size;
+    int32_t num_meshes, num_bvh_nodes; /* nodes of the four-wide BVH     */
+    int32_t bvh_depth, max_leaf_size;  /* wide nodes on the longest path  */
     uint64_t device_bytes;   /* device memory held by the scene             */
     uint64_t upload_bytes;   /* bytes copied host->device by one upload     */
     float env[3];            /* constant radiance seen by escaping rays     */
@@ -310,9 +310,11 @@ AQUA_API aqua_status aqua_convert_obj(aqua_ctx* ctx, const char* obj_path, const
  * clamped to [0, 1]. */
 AQUA_API aqua_status aqua_write_image(aqua_ctx* ctx, const char* path, const float* rgb, int32_t width,
                                       int32_t height);
-/* The flattened BVH as the device holds it: nodes = 16 floats per node (four
- * 16-byte words, layout in bvh.h), tri_order[k] = scene index of the k-th
- * triangle in leaf order. */
+/* The flattened BVH as the device holds it: a four-wide tree, nodes = 32
+ * floats per node (eight 16-byte words: lo.x, hi.x, lo.y, hi.y, lo.z, hi.z of
+ * the four child boxes, then the four child links and the four leaf counts as
+ * int32; layout in bvh.h), tri_order[k] = scene index of the k-th triangle in
+ * leaf order. */
 AQUA_API aqua_status aqua_scene_export_bvh(aqua_ctx* ctx, const aqua_scene* scene,
                                            float* nodes, int32_t* tri_order);
 

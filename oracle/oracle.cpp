@@ -8,9 +8,11 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <thread>
+#include <utility>
 #include <vector>
 
 namespace {
@@ -151,13 +153,42 @@ bool hit_d(V3<double> o, V3<double> d, const Tri& tr, double tmin, double tmax, 
 }
 
 // ------------------------------------------------------------------ BVH walk
-// Visits the flattened BVH exactly as the device kernels do; calls
-// leaf(first, count) for every leaf reached, box(tfar) returns the current
-// far limit. Templated on the box test.
-struct Node {
-    float w[16];
-};
-inline const float* node_at(const orc_scene* s, int32_t i) { return s->nodes + 16 * (size_t)i; }
+// Walks the exported BVH in the order of the device's canonical traversal
+// (csrc/device.cuh, traverse): same nodes, same box tests, same counts.
+inline const float* node_at(const orc_scene* s, int32_t i) { return s->nodes + 32 * (size_t)i; }
+
+// Four-wide node (32 floats: lo.x, hi.x, lo.y, hi.y, lo.z, hi.z of the four
+// child boxes, then the child links as int32). Restates the device's
+// visit_wide (csrc/device.cuh): entry distances of the four boxes, the same
+// five-comparator ordering network (ties keep slot order), the hit children
+// but the nearest pushed farthest first; returns the nearest child, else the
+// top of the stack, else kDone.
+constexpr int32_t kDone = std::numeric_limits<int32_t>::min();
+constexpr int kStack = 128;  // the library refuses trees needing 96 or more
+template <class T, class Entry>
+int32_t visit_wide(const float* w, Entry&& entry, int32_t* stack, int& sp) {
+    T t[4];
+    int32_t c[4];
+    for (int k = 0; k < 4; ++k) {
+        t[k] = entry(w[k], w[4 + k], w[8 + k], w[12 + k], w[16 + k], w[20 + k]);
+        memcpy(&c[k], &w[24 + k], 4);
+    }
+    auto ce = [&](int a, int b) {
+        if (t[b] < t[a]) {
+            std::swap(t[a], t[b]);
+            std::swap(c[a], c[b]);
+        }
+    };
+    ce(0, 1); ce(2, 3); ce(0, 2); ce(1, 3); ce(1, 2);
+    const T inf = std::numeric_limits<T>::infinity();
+    for (int k = 3; k >= 1; --k)
+        if (t[k] != inf) {
+            if (sp >= kStack) abort();
+            stack[sp++] = c[k];
+        }
+    if (t[0] != inf) return c[0];
+    return sp > 0 ? stack[--sp] : kDone;
+}
 
 struct RayF {
     V3<float> o, d, invd;
@@ -168,9 +199,9 @@ inline float inv_safe(float d) {
     float dd = ad < 1e-20f ? (d < 0.0f ? -1e-20f : 1e-20f) : d;
     return 1.0f / dd;
 }
-inline float entry_f(const float* lo_hi_xy, float loz, float hiz, const RayF& r, float tlim) {
-    float tx0 = (lo_hi_xy[0] - r.o.x) * r.invd.x, tx1 = (lo_hi_xy[1] - r.o.x) * r.invd.x;
-    float ty0 = (lo_hi_xy[2] - r.o.y) * r.invd.y, ty1 = (lo_hi_xy[3] - r.o.y) * r.invd.y;
+inline float entry_f(float lox, float hix, float loy, float hiy, float loz, float hiz, const RayF& r, float tlim) {
+    float tx0 = (lox - r.o.x) * r.invd.x, tx1 = (hix - r.o.x) * r.invd.x;
+    float ty0 = (loy - r.o.y) * r.invd.y, ty1 = (hiy - r.o.y) * r.invd.y;
     float tz0 = (loz - r.o.z) * r.invd.z, tz1 = (hiz - r.o.z) * r.invd.z;
     float tn = mx(mx(mn(tx0, tx1), mn(ty0, ty1)), mx(mn(tz0, tz1), r.tmin));
     float tf = mn(mn(mx(tx0, tx1), mx(ty0, ty1)), mn(mx(tz0, tz1), tlim));
@@ -187,30 +218,18 @@ HitF trace_f(const orc_scene* s, V3<float> o, V3<float> d, float tmin, float tma
     RayF r{o, d, {inv_safe(d.x), inv_safe(d.y), inv_safe(d.z)}, tmin, tmax};
     ShearF sh = shear_f(o, d);
     HitF h{tmax, 0, 0, -1, 0x7fffffff, 0, 0};
-    int32_t stack[64];
+    int32_t stack[kStack];
     int sp = 0;
     int32_t node = 0;
-    const float inf = std::numeric_limits<float>::infinity();
+    auto entry = [&](float lx, float hx, float ly, float hy, float lz, float hz) {
+        return entry_f(lx, hx, ly, hy, lz, hz, r, h.t);
+    };
     while (true) {
         while (node >= 0) {
-            const float* w = node_at(s, node);
             h.nodes++;
-            float t0 = entry_f(w + 0, w[8], w[9], r, h.t);
-            float t1 = entry_f(w + 4, w[10], w[11], r, h.t);
-            int32_t c0, c1;
-            memcpy(&c0, &w[12], 4);
-            memcpy(&c1, &w[13], 4);
-            bool h0 = t0 != inf, h1 = t1 != inf;
-            if (h0 && h1) {
-                if (t1 < t0) { stack[sp++] = c0; node = c1; }
-                else { stack[sp++] = c1; node = c0; }
-            } else if (h0) node = c0;
-            else if (h1) node = c1;
-            else {
-                if (sp == 0) return h;
-                node = stack[--sp];
-            }
+            node = visit_wide<float>(node_at(s, node), entry, stack, sp);
         }
+        if (node == kDone) return h;
         int32_t code = ~node;
         int32_t first = code >> 3, cnt = code & 7;
         for (int k = 0; k < cnt; ++k) {
@@ -236,7 +255,7 @@ HitD trace_d(const orc_scene* s, V3<double> o, V3<double> d, double tmin, double
     V3<double> invd{1.0 / (std::fabs(d.x) < 1e-300 ? 1e-300 : d.x), 1.0 / (std::fabs(d.y) < 1e-300 ? 1e-300 : d.y),
                     1.0 / (std::fabs(d.z) < 1e-300 ? 1e-300 : d.z)};
     HitD h{tmax, 0, 0, -1};
-    int32_t stack[64];
+    int32_t stack[kStack];
     int sp = 0;
     int32_t node = 0;
     auto entry = [&](double lx, double hx, double ly, double hy, double lz, double hz) {
@@ -248,26 +267,9 @@ HitD trace_d(const orc_scene* s, V3<double> o, V3<double> d, double tmin, double
         tf *= 1.0 + 1e-12;
         return tn <= tf ? tn : std::numeric_limits<double>::infinity();
     };
-    const double inf = std::numeric_limits<double>::infinity();
     while (true) {
-        while (node >= 0) {
-            const float* w = node_at(s, node);
-            double t0 = entry(w[0], w[1], w[2], w[3], w[8], w[9]);
-            double t1 = entry(w[4], w[5], w[6], w[7], w[10], w[11]);
-            int32_t c0, c1;
-            memcpy(&c0, &w[12], 4);
-            memcpy(&c1, &w[13], 4);
-            bool h0 = t0 != inf, h1 = t1 != inf;
-            if (h0 && h1) {
-                if (t1 < t0) { stack[sp++] = c0; node = c1; }
-                else { stack[sp++] = c1; node = c0; }
-            } else if (h0) node = c0;
-            else if (h1) node = c1;
-            else {
-                if (sp == 0) return h;
-                node = stack[--sp];
-            }
-        }
+        while (node >= 0) node = visit_wide<double>(node_at(s, node), entry, stack, sp);
+        if (node == kDone) return h;
         int32_t code = ~node;
         int32_t first = code >> 3, cnt = code & 7;
         for (int k = 0; k < cnt; ++k) {

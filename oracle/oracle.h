@@ -31,7 +31,7 @@ extern "C" {
 #endif
 
 typedef struct orc_scene {
-    const float* nodes;        /* flattened BVH, 16 floats per node     */
+    const float* nodes;        /* four-wide BVH, 32 floats per node     */
     int32_t n_nodes;
     const int32_t* tri_order;  /* leaf order -> scene triangle          */
     const float* verts;        /* 9 floats per triangle, scene order    */
