@@ -192,7 +192,7 @@ __device__ __forceinline__ bool bounce(const DevScene& S, int max_depth, int rr_
 // 5 resident blocks of 256 (48 registers): the spilled path state costs less
 // than the latency the extra warps hide (measured: 423 -> 623 Mpaths/s on
 // the 64-job batch together with per-lane path regeneration).
-__global__ void __launch_bounds__(256, 5) k_batch(const DevScene* __restrict__ scenes, const DevJob* __restrict__ jobs, int njobs,
+__global__ void __launch_bounds__(256, 4) k_batch(const DevScene* __restrict__ scenes, const DevJob* __restrict__ jobs, int njobs,
                         uint32_t total_pixels, uint32_t* __restrict__ counters,
                         unsigned long long* __restrict__ clocks, unsigned long long* __restrict__ stats) {
     __shared__ float lut[256];

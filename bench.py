@@ -604,9 +604,9 @@ def main():
     ap.add_argument("--no-interior", action="store_true", help="skip the 1080p interior measurement")
     # dram__bytes_read.sum + dram__bytes_write.sum of one full-queue
     # k_trace_ext launch (1M rays) of this workload, from `ncu --set full`
-    # (41.46 MB read + 4.01 MB written); every launch of the step has the
+    # (41.53 MB read + 4.16 MB written); every launch of the step has the
     # same queue size until the last samples drain.
-    ap.add_argument("--traffic-per-launch", type=float, default=45.47e6,
+    ap.add_argument("--traffic-per-launch", type=float, default=45.70e6,
                     help="DRAM bytes per k_trace_ext launch from an ncu capture")
     ap.add_argument("--spp", type=int, default=0,
                     help="samples per pixel of the workload (default 1024; smaller only for profiling captures)")
