@@ -38,12 +38,19 @@ __device__ __forceinline__ unsigned long long device_clock_ns() {
     return t;
 }
 
-// The state of a lane's path between bounces.
+// The state of a lane's path between rays. A lane traces one ray per loop
+// iteration: the path's extension ray (o, dir), or, when `shadow` is set,
+// the shadow ray of the last vertex's light sample (from o along sdir up to
+// stmax), whose contribution is added when it is unoccluded; `alive` then
+// says whether the path goes on with the extension ray (o, dir) afterwards.
 struct LanePath {
     v3 o, dir, thr;
     float pdf_b;
     int depth;
     uint64_t st, inc;
+    v3 sdir, contrib;
+    float stmax;
+    bool shadow, alive;
 };
 
 // Camera ray of sample `sample` of `pixel`.
@@ -55,143 +62,152 @@ __device__ __forceinline__ void start_sample(const DevJob& J, uint32_t pixel, ui
     P.thr = mk(1.0f, 1.0f, 1.0f);
     P.pdf_b = 0.0f;
     P.depth = 0;
+    P.shadow = false;
+    P.alive = true;
 }
 
-// One bounce: closest hit, emission with MIS, next-event estimation with an
-// any-hit shadow ray, BSDF sampling and Russian roulette. Contributions are
-// added to `sum` in the wavefront's order. Returns false when the path ends.
-__device__ __forceinline__ bool bounce(const DevScene& S, int max_depth, int rr_depth, const float* lut,
-                                       LanePath& P, v3& sum, uint32_t& n_ext, uint32_t& n_shadow) {
-    v3& o = P.o;
-    v3& dir = P.dir;
-    v3& thr = P.thr;
-    float& pdf_b = P.pdf_b;
-    uint64_t& st = P.st;
-    const uint64_t inc = P.inc;
-    const int depth = P.depth;
-    {
-        ++n_ext;
-        TraceResult h = traverse_fast<false>(S, o, dir, 0.0f, INFINITY);
-        if (h.tri < 0) {
-            v3 e = mk(S.env[0], S.env[1], S.env[2]);
-            if (e.x > 0.0f || e.y > 0.0f || e.z > 0.0f) sum = sum + thr * e;
-            return false;
-        }
-        const float4* tw = S.tris + 3 * (size_t)h.tri;
-        float4 a = ldg_(tw), b = ldg_(tw + 1), c = ldg_(tw + 2);
-        uint32_t info = (uint32_t)__float_as_int(b.w);
-        v3 v0 = f3(a), e1 = f3(b) - v0, e2 = f3(c) - v0;
-        v3 p = v0 + e1 * h.u + e2 * h.v;
-        v3 ng = normalize(cross(e1, e2));
-        v3 wo = -dir;
-        int light = (int)(info >> 16) - 1;
-        if (light >= 0) {
-            DevLight L = S.lights[light];
-            v3 nl = normalize(cross(f3(L.e1), f3(L.e2)));
-            float cos_l = dot(nl, wo);
-            if (cos_l > 0.0f) {
-                float w = 1.0f;
-                if (depth > 0 && pdf_b > 0.0f) {
-                    float pl = L.e2.w * h.t * h.t / (L.e1.w * cos_l);
-                    w = power_heuristic(pdf_b, pl);
-                }
-                sum = sum + thr * f3(L.le) * w;
-            }
-        }
-        if (depth >= max_depth) return false;
-        if (dot(ng, wo) < 0.0f) ng = -ng;
-        const v3 ns = shading_normal(S, h.tri, h.u, h.v, ng, wo);
-        DevMaterial m = S.mats[info & 0xffffu];
-        v3 base = f3(m.a);
-        int ti = __float_as_int(m.a.w);
-        if (ti >= 0) {
-            const float2* uv = S.uvs + 3 * (size_t)h.tri;
-            float2 t0 = ldg_(uv), t1 = ldg_(uv + 1), t2 = ldg_(uv + 2);
-            float w0 = 1.0f - h.u - h.v;
-            float tu = t0.x * w0 + t1.x * h.u + t2.x * h.v;
-            float tv = t0.y * w0 + t1.y * h.u + t2.y * h.v;
-            base = base * tex_bilinear(S, ti, tu, tv, lut);
-        }
-        Bsdf B = make_bsdf(base, m.b.x, m.b.y, m.b.z);
-        v3 T, Bt;
-        onb(ns, T, Bt);
-        v3 wol = mk(dot(wo, T), dot(wo, Bt), dot(wo, ns));
-        float u[kBounceDims];
-#pragma unroll
-        for (int k = 0; k < kBounceDims; ++k) u[k] = draw(st, inc);
-        if (S.n_lights > 0 && wol.z > 0.0f) {
-            DevLight L = S.lights[pick_light(S, u[0])];
-            int ty = __float_as_int(L.p0.w);
-            float pmf = L.e2.w;
-            v3 contrib = mk(0, 0, 0), wi;
-            float dist = 0.0f;
-            if (ty == AQUA_LIGHT_POINT) {
-                v3 dl = f3(L.p0) - p;
-                float d2 = dot(dl, dl);
-                dist = sqrtf(d2);
-                wi = dl * (1.0f / dist);
-                float cs = dot(wi, ns), cg = dot(wi, ng);
-                if (cs > 0.0f && cg > 0.0f && d2 > 0.0f) {
-                    v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
-                    contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs / (d2 * pmf));
-                }
-            } else {
-                v3 le1 = f3(L.e1), le2 = f3(L.e2), xl;
-                if (ty == AQUA_LIGHT_QUAD) {
-                    xl = f3(L.p0) + le1 * u[1] + le2 * u[2];
-                } else {
-                    float su = sqrtf(u[1]);
-                    xl = f3(L.p0) + le1 * (su * (1.0f - u[2])) + le2 * (su * u[2]);
-                }
-                v3 nl = normalize(cross(le1, le2));
-                v3 dl = xl - p;
-                float d2 = dot(dl, dl);
-                dist = sqrtf(d2);
-                wi = dl * (1.0f / dist);
-                float cl = -dot(wi, nl), cs = dot(wi, ns), cg = dot(wi, ng);
-                if (cl > 0.0f && cs > 0.0f && cg > 0.0f && d2 > 0.0f) {
-                    v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
-                    float pl = pmf * d2 / (L.e1.w * cl);
-                    float pb = bsdf_pdf(B, wol, wil);
-                    float w = power_heuristic(pl, pb);
-                    contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs * w / pl);
-                }
-            }
-            if (contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f) {
-                ++n_shadow;
-                v3 so = offset_ray(p, ng);
-                TraceResult sh = traverse_fast<true>(S, so, wi, 0.0f, dist * (1.0f - 1e-4f));
-                if (sh.tri < 0) sum = sum + contrib;
-            }
-        }
-        v3 wil = bsdf_sample(B, wol, u[3], u[4], u[5]);
-        if (!(wil.z > 0.0f && wol.z > 0.0f)) return false;
-        float pdf = bsdf_pdf(B, wol, wil);
-        v3 f = bsdf_eval(B, wol, wil);
-        if (!(pdf > 0.0f)) return false;
-        thr = thr * f * (wil.z / pdf);
-        bool ok = maxc(thr) > 0.0f && isfinite(thr.x) && isfinite(thr.y) && isfinite(thr.z);
-        if (ok && depth >= rr_depth) {
-            float q = fminf(1.0f, maxc(thr));
-            if (u[6] >= q) ok = false;
-            else thr = thr * (1.0f / q);
-        }
-        if (!ok) return false;
-        dir = normalize(T * wil.x + Bt * wil.y + ns * wil.z);
-        if (S.nrm && !(dot(dir, ng) > 0.0f)) return false;  // below the geometric surface
-        o = offset_ray(p, ng);
-        pdf_b = pdf;
-        P.depth = depth + 1;
-        return true;
+// BSDF sampling and Russian roulette at shading point p: the next extension
+// ray, or false when the path ends.
+__device__ __forceinline__ bool continue_path(const Bsdf& B, v3 wol, const float* u, v3 T, v3 Bt, v3 ns, v3 ng,
+                                              v3 p, bool smooth, int rr_depth, LanePath& P) {
+    v3 wil = bsdf_sample(B, wol, u[3], u[4], u[5]);
+    if (!(wil.z > 0.0f && wol.z > 0.0f)) return false;
+    float pdf = bsdf_pdf(B, wol, wil);
+    v3 f = bsdf_eval(B, wol, wil);
+    if (!(pdf > 0.0f)) return false;
+    v3 thr = P.thr * f * (wil.z / pdf);
+    bool ok = maxc(thr) > 0.0f && isfinite(thr.x) && isfinite(thr.y) && isfinite(thr.z);
+    if (ok && P.depth >= rr_depth) {
+        float q = fminf(1.0f, maxc(thr));
+        if (u[6] >= q) ok = false;
+        else thr = thr * (1.0f / q);
     }
+    if (!ok) return false;
+    const v3 dir = normalize(T * wil.x + Bt * wil.y + ns * wil.z);
+    if (smooth && !(dot(dir, ng) > 0.0f)) return false;  // below the geometric surface
+    P.thr = thr;
+    P.dir = dir;
+    P.o = offset_ray(p, ng);
+    P.pdf_b = pdf;
+    P.depth = P.depth + 1;
+    return true;
+}
+
+// The vertex a closest-hit ray found: emission with MIS, next-event
+// estimation (schedules the shadow ray of one light sample), BSDF sampling
+// and Russian roulette. Contributions are added to `sum` in the wavefront's
+// order (the light sample's once its shadow ray is traced). Returns false
+// when the path ends (a scheduled shadow ray is still traced).
+__device__ __forceinline__ bool shade_hit(const DevScene& S, int max_depth, int rr_depth, const float* lut,
+                                          const TraceResult& h, LanePath& P, v3& sum) {
+    const v3 thr = P.thr;
+    const int depth = P.depth;
+    if (h.tri < 0) {
+        v3 e = mk(S.env[0], S.env[1], S.env[2]);
+        if (e.x > 0.0f || e.y > 0.0f || e.z > 0.0f) sum = sum + thr * e;
+        return false;
+    }
+    const float4* tw = S.tris + 3 * (size_t)h.tri;
+    float4 a = ldg_(tw), b = ldg_(tw + 1), c = ldg_(tw + 2);
+    uint32_t info = (uint32_t)__float_as_int(b.w);
+    v3 v0 = f3(a), e1 = f3(b) - v0, e2 = f3(c) - v0;
+    v3 p = v0 + e1 * h.u + e2 * h.v;
+    v3 ng = normalize(cross(e1, e2));
+    v3 wo = -P.dir;
+    int light = (int)(info >> 16) - 1;
+    if (light >= 0) {
+        DevLight L = S.lights[light];
+        v3 nl = normalize(cross(f3(L.e1), f3(L.e2)));
+        float cos_l = dot(nl, wo);
+        if (cos_l > 0.0f) {
+            float w = 1.0f;
+            if (depth > 0 && P.pdf_b > 0.0f) {
+                float pl = L.e2.w * h.t * h.t / (L.e1.w * cos_l);
+                w = power_heuristic(P.pdf_b, pl);
+            }
+            sum = sum + thr * f3(L.le) * w;
+        }
+    }
+    if (depth >= max_depth) return false;
+    if (dot(ng, wo) < 0.0f) ng = -ng;
+    const v3 ns = shading_normal(S, h.tri, h.u, h.v, ng, wo);
+    DevMaterial m = S.mats[info & 0xffffu];
+    v3 base = f3(m.a);
+    int ti = __float_as_int(m.a.w);
+    if (ti >= 0) {
+        const float2* uv = S.uvs + 3 * (size_t)h.tri;
+        float2 t0 = ldg_(uv), t1 = ldg_(uv + 1), t2 = ldg_(uv + 2);
+        float w0 = 1.0f - h.u - h.v;
+        float tu = t0.x * w0 + t1.x * h.u + t2.x * h.v;
+        float tv = t0.y * w0 + t1.y * h.u + t2.y * h.v;
+        base = base * tex_bilinear(S, ti, tu, tv, lut);
+    }
+    Bsdf B = make_bsdf(base, m.b.x, m.b.y, m.b.z);
+    v3 T, Bt;
+    onb(ns, T, Bt);
+    v3 wol = mk(dot(wo, T), dot(wo, Bt), dot(wo, ns));
+    float u[kBounceDims];
+#pragma unroll
+    for (int k = 0; k < kBounceDims; ++k) u[k] = draw(P.st, P.inc);
+    if (S.n_lights > 0 && wol.z > 0.0f) {
+        DevLight L = S.lights[pick_light(S, u[0])];
+        int ty = __float_as_int(L.p0.w);
+        float pmf = L.e2.w;
+        v3 contrib = mk(0, 0, 0), wi;
+        float dist = 0.0f;
+        if (ty == AQUA_LIGHT_POINT) {
+            v3 dl = f3(L.p0) - p;
+            float d2 = dot(dl, dl);
+            dist = sqrtf(d2);
+            wi = dl * (1.0f / dist);
+            float cs = dot(wi, ns), cg = dot(wi, ng);
+            if (cs > 0.0f && cg > 0.0f && d2 > 0.0f) {
+                v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
+                contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs / (d2 * pmf));
+            }
+        } else {
+            v3 le1 = f3(L.e1), le2 = f3(L.e2), xl;
+            if (ty == AQUA_LIGHT_QUAD) {
+                xl = f3(L.p0) + le1 * u[1] + le2 * u[2];
+            } else {
+                float su = sqrtf(u[1]);
+                xl = f3(L.p0) + le1 * (su * (1.0f - u[2])) + le2 * (su * u[2]);
+            }
+            v3 nl = normalize(cross(le1, le2));
+            v3 dl = xl - p;
+            float d2 = dot(dl, dl);
+            dist = sqrtf(d2);
+            wi = dl * (1.0f / dist);
+            float cl = -dot(wi, nl), cs = dot(wi, ns), cg = dot(wi, ng);
+            if (cl > 0.0f && cs > 0.0f && cg > 0.0f && d2 > 0.0f) {
+                v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
+                float pl = pmf * d2 / (L.e1.w * cl);
+                float pb = bsdf_pdf(B, wol, wil);
+                float w = power_heuristic(pl, pb);
+                contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs * w / pl);
+            }
+        }
+        if (contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f) {
+            // The shadow ray leaves from the same offset point as the
+            // extension ray.
+            P.shadow = true;
+            P.o = offset_ray(p, ng);
+            P.sdir = wi;
+            P.stmax = dist * (1.0f - 1e-4f);
+            P.contrib = contrib;
+        }
+    }
+    const bool alive = continue_path(B, wol, u, T, Bt, ns, ng, p, S.nrm != nullptr, rr_depth, P);
+    P.alive = alive;
+    return alive;
 }
 
 // Persistent kernel over all jobs' pixels. counters[0] = next pixel of the
 // whole batch, counters[1 + j] = finished pixels of job j. clocks[0] = launch
 // time, clocks[1 + j] = completion time of job j.
-// 5 resident blocks of 256 (48 registers): the spilled path state costs less
-// than the latency the extra warps hide (measured: 423 -> 623 Mpaths/s on
-// the 64-job batch together with per-lane path regeneration).
+// 4 resident blocks of 256 (64 registers): the spilled path state costs less
+// than the latency the extra warps hide (measured on the 64-job batch: 48,
+// 64 and 80 registers and the compiler's own 107 compared).
 __global__ void __launch_bounds__(256, 4) k_batch(const DevScene* __restrict__ scenes, const DevJob* __restrict__ jobs, int njobs,
                         uint32_t total_pixels, uint32_t* __restrict__ counters,
                         unsigned long long* __restrict__ clocks, unsigned long long* __restrict__ stats) {
@@ -240,7 +256,23 @@ __global__ void __launch_bounds__(256, 4) k_batch(const DevScene* __restrict__ s
         if (!__any_sync(kFull, have)) break;
         if (!have) continue;
         const DevJob& J = jobs[job];
-        if (bounce(scenes[J.scene], J.max_depth, J.rr_depth, lut, P, sum, n_ext, n_sh)) continue;
+        const DevScene& S = scenes[J.scene];
+        // One ray per iteration, from one call site: the pending shadow ray,
+        // else the extension ray.
+        const bool any = P.shadow;
+        if (any) ++n_sh;
+        else ++n_ext;
+        const TraceResult h = traverse_fast(S, P.o, any ? P.sdir : P.dir, 0.0f, any ? P.stmax : INFINITY, any);
+        bool alive;
+        if (any) {
+            if (h.tri < 0) sum = sum + P.contrib;
+            P.shadow = false;
+            alive = P.alive;
+        } else {
+            alive = shade_hit(S, J.max_depth, J.rr_depth, lut, h, P, sum);
+            if (P.shadow) continue;
+        }
+        if (alive) continue;
         // The path ended: the pixel's next sample, or the pixel is done.
         if (++sample < (uint32_t)J.spp) {
             start_sample(J, pixel, sample, P);

@@ -171,9 +171,11 @@ __device__ __forceinline__ TraceResult traverse(const DevScene& S, v3 o, v3 d, f
 // holds a leaf (warp vote), then all test triangles together. Boxes, culling
 // and triangle tests are those of traverse(), so the result (the minimum
 // (t, scene index) over all triangles hit, or any hit) is identical; only
-// the order of visits, and thus the work counts, differ.
-template <bool ANY>
-__device__ __forceinline__ TraceResult traverse_fast(const DevScene& S, v3 o, v3 d, float tmin, float tmax) {
+// the order of visits, and thus the work counts, differ. `any` (stop at the
+// first hit) is a run-time flag, so a kernel that traces both kinds of ray
+// from one call site holds one inlined copy of the walk.
+__device__ __forceinline__ TraceResult traverse_fast(const DevScene& S, v3 o, v3 d, float tmin, float tmax,
+                                                     bool any) {
     RayPre rp;
     rp.o = o;
     rp.invd = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
@@ -203,7 +205,7 @@ __device__ __forceinline__ TraceResult traverse_fast(const DevScene& S, v3 o, v3
                 TriHit h = intersect_tri(sh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), tmin, tmax);
                 if (h.hit) {
                     int32_t id = __float_as_int(a.w);
-                    if (ANY) {
+                    if (any) {
                         r.t = h.t; r.tri = first + k; r.id = id;
                         return r;
                     }

@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(128) k_trace_user(DevScene S, const float4* __
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         float4 a = ldg_(rays + 2 * i), b = ldg_(rays + 2 * i + 1);
         store(i, COUNT ? traverse<ANY, true>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, nodes, tris)
-                       : traverse_fast<ANY>(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w));
+                       : traverse_fast(S, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, ANY));
     }
     if (COUNT) {
         for (int o = 16; o > 0; o >>= 1) {
