@@ -223,7 +223,7 @@ static void need_device(aqua_ctx* ctx) {
 
 extern "C" {
 
-AQUA_API int aqua_version(void) { return 100; }
+AQUA_API int aqua_version(void) { return AQUA_VERSION; }
 
 AQUA_API const char* aqua_status_string(aqua_status s) {
     switch (s) {

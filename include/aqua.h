@@ -231,6 +231,10 @@ AQUA_API void aqua_destroy(aqua_ctx* ctx);
  * next call on ctx. aqua_create failures are reported by aqua_last_error(NULL). */
 AQUA_API const char* aqua_last_error(const aqua_ctx* ctx);
 AQUA_API const char* aqua_status_string(aqua_status s);
+/* ABI version: 100 x major + minor. Major 2: aqua_scene_export_bvh returns
+ * the four-wide tree (32 floats per node; major 1 returned a binary tree of
+ * 16 floats per node). */
+#define AQUA_VERSION 200
 AQUA_API int aqua_version(void);
 
 /* ---------------------------------------------------------------- scenes */

@@ -54,7 +54,7 @@ def test_struct_layouts():
 
 def test_status_strings_and_version():
     lib = aqua.load_library()
-    assert lib.aqua_version() >= 100
+    assert lib.aqua_version() == 200  # four-wide BVH export layout
     assert lib.aqua_status_string(0) == b"ok"
     assert lib.aqua_status_string(4) == b"missing asset"
     assert lib.aqua_status_string(99) == b"unknown status"
