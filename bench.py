@@ -498,6 +498,7 @@ def run_gpu(args, world, rank, local, pg):
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     barrier(pg)
+    ws_mb = ctx.workspace_bytes() / 1e6  # this workload's wavefront state, before the side runs grow it
     dev_ms = sum(s.device_ms for s in steps)
     ms_max = max_over_ranks(pg, dev_ms)
     paths = sum(s.paths for s in steps)
@@ -566,7 +567,7 @@ def run_gpu(args, world, rank, local, pg):
                 "data": "synthetic (procedural Cornell box, seeded)",
                 "config": dict(WORKLOAD, parallelism=f"replicas x{world}",
                                l2="256 MB buffer zeroed before every timed step; wavefront state "
-                                  f"{ctx.workspace_bytes() / 1e6:.0f} MB > 129 MB L2"),
+                                  f"{ws_mb:.0f} MB > 129 MB L2"),
                 "mrays_per_s": sum_over_ranks(pg, sum(s.ext_rays + s.shadow_rays for s in steps)) /
                                (ms_max * 1e-3) / 1e6,
                 "wall_s": wall, "clocks": clk.summary(), "roofline": roofline, "cpu_baseline": cpu,
