@@ -112,9 +112,28 @@ def soup(kind: str, rng):
     return v
 
 
+def aimed_rays(v, n, rng):
+    """Rays from around the triangles' bounding box towards points on the
+    triangles themselves, so that most of them hit."""
+    lo, hi = v.reshape(-1, 3).min(0), v.reshape(-1, 3).max(0)
+    ext = np.maximum(hi - lo, 1e-3)
+    tri = v[rng.integers(0, v.shape[0], n)]
+    w = rng.dirichlet(np.ones(3), n)
+    target = np.einsum("nk,nka->na", w, tri)
+    org = lo - 0.5 * ext + rng.uniform(0, 1, (n, 3)) * 2 * ext
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = org
+    rays[:, 4:7] = target - org
+    rays[:, 7] = np.inf
+    return rays
+
+
 @pytest.mark.parametrize("kind", ["one", "coincident", "chain", "cloud"])
 def test_stress_trees(host_ctx, tmp_path, kind):
-    v = soup(kind, np.random.default_rng(7))
+    import pyoracle
+
+    rng = np.random.default_rng(7)
+    v = soup(kind, rng)
     verts = v.reshape(-1, 3)
     idx = np.arange(verts.shape[0]).reshape(-1, 3)
     write_mesh(tmp_path / "m.mesh", verts.tolist(), idx.tolist(), normals=False)
@@ -123,4 +142,18 @@ def test_stress_trees(host_ctx, tmp_path, kind):
     s = host_ctx.load_scene(str(p))
     assert s.info().num_triangles == idx.shape[0]
     check_tree(s)
+    # The oracle's walk of this tree equals brute force bit for bit
+    # (coincident triangles: the smallest scene index wins the tie).
+    o = pyoracle.OracleScene.from_aqua(s)
+    rays = aimed_rays(v.astype(np.float32), 4000, rng)
+    t, u, _, prim, _ = o.trace_bvh_f32(rays)
+    tb, ub, _, pb = o.trace_brute_f32(rays)
+    np.testing.assert_array_equal(prim, pb)
+    np.testing.assert_array_equal(t.view(np.uint32), tb.view(np.uint32))
+    np.testing.assert_array_equal(u.view(np.uint32), ub.view(np.uint32))
+    assert np.mean(prim >= 0) > 0.5
+    occ = o.trace_bvh_f32(rays, any_hit=True)[3]
+    np.testing.assert_array_equal(occ >= 0, pb >= 0)
+    if kind == "coincident":
+        assert set(prim[prim >= 0].tolist()) == {0}
     s.free()
