@@ -169,3 +169,31 @@ def test_device_pointer_path(gpu_ctx, cornell):
     ot, _, _, oprim, _ = o.trace_bvh_f32(rays)
     assert np.array_equal(h[:, 3].view(np.int32), oprim)
     assert np.array_equal(h[:, 0], ot)
+
+
+@pytest.mark.parametrize("kind", ["coincident", "chain", "cloud"])
+def test_degenerate_triangle_sets_bit_exact(gpu_ctx, tmp_path, kind):
+    """Ties and degenerate trees: 37 coincident triangles (every hit a tie,
+    broken by the smaller scene index), a chain of thin triangles whose sizes
+    span six decades, a dense random cloud. Closest and any hit, both device
+    traversals against the oracle's walk."""
+    import pyoracle
+    from test_bvh_structure import aimed_rays, soup
+    from test_loaders import principled, scene_json, write_mesh
+
+    rng = np.random.default_rng(11)
+    v = soup(kind, rng)
+    verts = v.reshape(-1, 3)
+    idx = np.arange(verts.shape[0]).reshape(-1, 3)
+    write_mesh(tmp_path / "m.mesh", verts.tolist(), idx.tolist(), normals=False)
+    p = tmp_path / "s.json"
+    p.write_text(json.dumps(scene_json([("m.mesh", "w")], {"w": principled()})))
+    s = gpu_ctx.load_scene(str(p))
+    o = pyoracle.OracleScene.from_aqua(s)
+    rays = aimed_rays(v.astype(np.float32), 20_000, rng)
+    prim, _ = assert_bit_exact(gpu_ctx, s, o, rays)
+    assert np.mean(prim >= 0) > 0.5
+    if kind == "coincident":
+        assert set(prim[prim >= 0].tolist()) == {0}
+    assert_bit_exact(gpu_ctx, s, o, rays, any_hit=True)
+    s.free()
