@@ -5,7 +5,7 @@
  * src/lib.rs is empty. Its de-facto contract is the on-disk data it ships:
  *   - scene JSON        scenes/cbox.json:1-628, scenes/room.json:1-3900
  *   - integrator JSON   scenes/integrator.json:1-9
- *   - BSON `.mesh`      scenes/*.mesh (name, vertices, normals, texcoords, indices)
+ *   - BSON `.mesh`      scenes/<name>.mesh (name, vertices, normals, texcoords, indices)
  * Each entry point below names the part of that contract (file:line) it serves.
  * A Rust `extern "C"` crate binds these 1:1 (no torch types, plain pointers and
  * sizes, no exceptions across the boundary).
