@@ -372,7 +372,7 @@ class Context:
 
     def _check(self, st: int):
         if st != OK:
-            raise AquaError(st, self.lib.aqua_last_error(self.handle).decode())
+            raise AquaError(st, self.lib.aqua_last_error(self.handle).decode("utf-8", "replace"))
 
     def close(self):
         if self.handle:

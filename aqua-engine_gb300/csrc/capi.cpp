@@ -189,6 +189,42 @@ void scene_upload(aqua_ctx* ctx, aqua_scene* s) {
 using namespace aq;
 
 // ---------------------------------------------------------------- ABI helpers
+// Error text as aqua_last_error hands it out: messages quote parts of the
+// input (a malformed OBJ line, a file name), so bytes that are neither
+// printable ASCII nor part of a well-formed UTF-8 sequence are written as
+// \xNN, and the text is cut at 1024 bytes. Callers can decode it as UTF-8.
+static std::string clean_message(const char* m) {
+    std::string out;
+    const unsigned char* p = reinterpret_cast<const unsigned char*>(m);
+    const size_t n = strlen(m);
+    auto cont = [&](size_t i, unsigned lo, unsigned hi) { return i < n && p[i] >= lo && p[i] <= hi; };
+    size_t i = 0;
+    while (i < n && out.size() < 1024) {
+        const unsigned c = p[i];
+        size_t len = 0;
+        if (c >= 0x20 && c < 0x7f) len = 1;
+        else if (c >= 0xc2 && c <= 0xdf) len = cont(i + 1, 0x80, 0xbf) ? 2 : 0;
+        else if (c >= 0xe0 && c <= 0xef) {
+            const unsigned lo = c == 0xe0 ? 0xa0 : 0x80, hi = c == 0xed ? 0x9f : 0xbf;
+            len = cont(i + 1, lo, hi) && cont(i + 2, 0x80, 0xbf) ? 3 : 0;
+        } else if (c >= 0xf0 && c <= 0xf4) {
+            const unsigned lo = c == 0xf0 ? 0x90 : 0x80, hi = c == 0xf4 ? 0x8f : 0xbf;
+            len = cont(i + 1, lo, hi) && cont(i + 2, 0x80, 0xbf) && cont(i + 3, 0x80, 0xbf) ? 4 : 0;
+        }
+        if (len) {
+            out.append(m + i, len);
+            i += len;
+        } else {
+            static const char* hex = "0123456789abcdef";
+            out += "\\x";
+            out += hex[c >> 4];
+            out += hex[c & 15];
+            ++i;
+        }
+    }
+    return out;
+}
+
 template <class F>
 static aqua_status guard(aqua_ctx* ctx, F&& f) {
     if (!ctx) return AQUA_ERR_INVALID_ARG;
@@ -199,16 +235,16 @@ static aqua_status guard(aqua_ctx* ctx, F&& f) {
         f();
         return AQUA_OK;
     } catch (Error& e) {
-        ctx->err = e.what();
+        ctx->err = clean_message(e.what());
         return e.status;
     } catch (SceneError& e) {
-        ctx->err = e.what();
+        ctx->err = clean_message(e.what());
         return e.status;
     } catch (std::bad_alloc&) {
         ctx->err = "host allocation failed";
         return AQUA_ERR_OOM;
     } catch (std::exception& e) {
-        ctx->err = e.what();
+        ctx->err = clean_message(e.what());
         return AQUA_ERR_INVALID_ARG;
     }
 }

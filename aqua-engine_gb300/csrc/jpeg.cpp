@@ -62,6 +62,7 @@ bool build_huff(Huff& h, const uint8_t* bits, const uint8_t* vals, int nvals) {
         h.valptr[l] = k;
         h.mincode[l] = (int32_t)code;
         for (int i = 0; i < bits[l - 1]; ++i, ++k, ++code) {
+            if (code >= (1u << l)) return false;  // more codes than this length holds
             if (l <= 9) {
                 uint32_t base = code << (9 - l);
                 for (uint32_t j = 0; j < (1u << (9 - l)); ++j) {
@@ -70,7 +71,6 @@ bool build_huff(Huff& h, const uint8_t* bits, const uint8_t* vals, int nvals) {
                 }
             }
         }
-        if (code > (1u << l)) return false;  // codes overflow their length
         h.maxcode[l] = bits[l - 1] ? (int32_t)code - 1 : -1;
         code <<= 1;
     }

@@ -1,6 +1,7 @@
 // json.cpp — recursive-descent JSON parser (RFC 8259).
 #include "json.h"
 
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 
@@ -104,7 +105,9 @@ struct Parser {
             while (i < n && s[i] >= '0' && s[i] <= '9') ++i;
         }
         std::string tok(s + st, i - st);
-        return strtod(tok.c_str(), nullptr);
+        const double v = strtod(tok.c_str(), nullptr);
+        if (!std::isfinite(v)) fail("number out of range");
+        return v;
     }
     Json value() {
         if (++depth > 256) fail("nesting too deep");

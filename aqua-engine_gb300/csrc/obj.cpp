@@ -69,7 +69,8 @@ std::vector<std::string> tokens(const std::string& line) {
 double num(const std::string& s, const std::string& where) {
     char* end = nullptr;
     double v = std::strtod(s.c_str(), &end);
-    if (end == s.c_str() || *end) throw SceneError(AQUA_ERR_PARSE, where + ": bad number \"" + s + "\"");
+    if (end == s.c_str() || *end || !std::isfinite(v))
+        throw SceneError(AQUA_ERR_PARSE, where + ": bad number \"" + s + "\"");
     return v;
 }
 

@@ -186,6 +186,10 @@ MeshData parse_mesh_bson(const uint8_t* data, size_t n) {
     size_t nv = m.positions.size() / 3;
     for (int64_t ix : m.indices)
         if (ix < 0 || (size_t)ix >= nv) r.fail("index out of range");
+    // A NaN or infinite coordinate would poison box bounds and shading.
+    for (const std::vector<double>* v : {&m.positions, &m.normals, &m.texcoords})
+        for (double x : *v)
+            if (!std::isfinite(x)) r.fail("non-finite vertex attribute");
     if (!m.normals.empty() && m.normals.size() != m.positions.size()) m.normals.clear();
     if (!m.texcoords.empty() && m.texcoords.size() / 2 != nv) m.texcoords.clear();
     return m;

@@ -370,6 +370,17 @@ def test_refusals(ctx):
     assert e.value.status == aqua.ERR_UNSUPPORTED and "arithmetic" in str(e.value)
 
 
+@pytest.mark.parametrize("name", ["jpeg_dht_overflow_a.jpg", "jpeg_dht_overflow_b.jpg"])
+def test_overfull_huffman_table_is_refused(ctx, name):
+    """Mutated test-encoder output whose DHT lists more codes of a length
+    than that length holds (found by fuzzing: the decoder used to write its
+    9-bit lookup table out of bounds before noticing)."""
+    data = open(os.path.join(GOLDEN, name), "rb").read()
+    with pytest.raises(aqua.AquaError) as e:
+        ctx.decode_jpeg(data)
+    assert e.value.status == aqua.ERR_UNSUPPORTED and "Huffman" in str(e.value)
+
+
 # ---------------------------------------------------------------- reference textures vs nvJPEG
 FACTS = json.load(open(os.path.join(GOLDEN, "jpeg_facts.json")))["files"]
 

@@ -221,6 +221,34 @@ def test_bson_index_out_of_range(host_ctx, tmp_path):
     assert e.value.status == aqua.ERR_PARSE and "index" in e.value.message
 
 
+@pytest.mark.parametrize("field", ["vertices", "normals", "texcoords"])
+@pytest.mark.parametrize("bad", [float("nan"), float("inf"), float("-inf")])
+def test_non_finite_mesh_attributes_are_refused(host_ctx, tmp_path, field, bad):
+    v = [[0, 0, 0], [1, 0, 0], [0, 1, 0]]
+    n = [[0, 0, 1]] * 3
+    uv = [[0, 0], [1, 0], [0, 1]]
+    if field == "vertices":
+        v = [[0, 0, 0], [bad, 0, 0], [0, 1, 0]]
+    elif field == "normals":
+        n = [[0, 0, 1], [0, bad, 1], [0, 0, 1]]
+    else:
+        uv = [[0, 0], [1, bad], [0, 1]]
+    write_mesh(tmp_path / "q.mesh", v, [[0, 1, 2]], uvs=uv, normals=n)
+    p = tmp_path / "s.json"
+    p.write_text(json.dumps(scene_json([("q.mesh", "a")], {"a": principled()})))
+    with pytest.raises(aqua.AquaError) as e:
+        host_ctx.load_scene(str(p))
+    assert e.value.status == aqua.ERR_PARSE and "non-finite" in e.value.message
+
+
+def test_out_of_range_json_number_is_refused(host_ctx, quad_scene):
+    d, p = quad_scene
+    p.write_text(p.read_text().replace('"fov": 40.0', '"fov": 1e999'))
+    with pytest.raises(aqua.AquaError) as e:
+        host_ctx.load_scene(str(p))
+    assert e.value.status == aqua.ERR_PARSE and "out of range" in e.value.message
+
+
 def test_emissive_mesh_becomes_triangle_lights(host_ctx, tmp_path):
     write_mesh(tmp_path / "l.mesh", [[-1, 2, -1], [1, 2, -1], [1, 2, 1], [-1, 2, 1]], [[0, 2, 1], [0, 3, 2]])
     p = tmp_path / "s.json"

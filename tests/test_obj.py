@@ -167,6 +167,20 @@ def test_obj_errors(ctx, tmp_path):
     with pytest.raises(aqua.AquaError) as e:
         ctx.convert_obj(str(tmp_path / "two.obj"), str(tmp_path))
     assert e.value.status == aqua.ERR_PARSE
+    # A number made of bytes that are not UTF-8: the message quotes it with
+    # those bytes escaped, so the C string aqua_last_error returns is UTF-8.
+    (tmp_path / "bytes.obj").write_bytes(b"v 0 0 \x89\xff\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+    st = ctx.lib.aqua_convert_obj(ctx.handle, str(tmp_path / "bytes.obj").encode(), str(tmp_path).encode(),
+                                  b"s.json", 8, 8, None, None)
+    assert st == aqua.ERR_PARSE
+    raw = ctx.lib.aqua_last_error(ctx.handle)
+    msg = raw.decode("utf-8")  # strict: must not raise
+    assert "bad number" in msg and "\\x89\\xff" in msg
+    # strtod reads "nan" and "inf"; a vertex must be a finite number
+    write(tmp_path / "nan.obj", "v 0 0 nan\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+    with pytest.raises(aqua.AquaError) as e:
+        ctx.convert_obj(str(tmp_path / "nan.obj"), str(tmp_path))
+    assert e.value.status == aqua.ERR_PARSE and "bad number" in str(e.value)
 
 
 def test_write_image_pfm_and_ppm(ctx, tmp_path):
