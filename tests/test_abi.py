@@ -4,9 +4,11 @@ layout rules. No GPU needed."""
 from __future__ import annotations
 
 import ctypes
+import json
 import os
 import re
 import subprocess
+import sys
 
 import pytest
 
@@ -77,3 +79,48 @@ def test_defaults_follow_integrator_json():
     # scenes/integrator.json:3-7
     assert (c.spp, c.batch_size, c.max_depth, c.training_iters) == (4, 512, 5, 2048)
     assert abs(c.learning_rate - 1e-3) < 1e-9
+
+
+NULL_CHILD = r'''
+import sys, json, ctypes as C
+sys.path.insert(0, sys.argv[1])
+import aqua
+lib = aqua.load_library()
+ctx = aqua.Context(device=-2)
+out = {}
+for mode in ("null_ctx", "host_ctx"):
+    for name, res, args in aqua.SIGNATURES:
+        if name in ("aqua_version", "aqua_render_noalloc_max_pixels", "aqua_status_string", "aqua_last_error"):
+            continue
+        vals = [0 if a in (C.c_int, C.c_int32, C.c_uint32, C.c_uint64, C.c_size_t) else None for a in args]
+        takes_ctx = bool(args) and args[0] is aqua._P and name not in ("aqua_destroy", "aqua_nrc_defaults")
+        if mode == "host_ctx" and takes_ctx:
+            vals[0] = ctx.handle
+        r = getattr(lib, name)(*vals)
+        out[mode + ":" + name] = r
+print(json.dumps(out))
+'''
+
+
+def test_every_entry_point_survives_null_arguments(built):
+    """Each entry point called with NULL pointers and zero sizes, once with a
+    NULL context and once with a host-only one: status calls return an error
+    (freeing or destroying NULL is a no-op that succeeds), the *_defaults
+    and destroy calls return quietly, and nothing crashes (child process)."""
+    r = subprocess.run([sys.executable, "-c", NULL_CHILD, os.path.join(ROOT, "aqua-engine_gb300")],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = json.loads(r.stdout.strip().splitlines()[-1])
+    noops = {"host_ctx:aqua_scene_free", "host_ctx:aqua_nrc_destroy"}
+    for key, st in got.items():
+        name = key.split(":")[1]
+        if name in ("aqua_destroy", "aqua_integrator_defaults", "aqua_tuning_defaults", "aqua_nrc_defaults"):
+            assert st is None, key
+        elif name == "aqua_workspace_bytes":
+            assert st == 0, key
+        elif key in noops:
+            assert st == aqua.OK, key
+        else:
+            assert st not in (None, aqua.OK), key
+            if key.startswith("null_ctx:"):
+                assert st == aqua.ERR_INVALID_ARG, key
