@@ -427,6 +427,18 @@ Bsdf_ read_bsdf(const Json& j, const std::string& dir, bool allow_missing, const
         if (t.image) throw SceneError(AQUA_ERR_UNSUPPORTED, "bsdf \"" + name + "\": image-valued emission");
         b.emission = t.value;
     }
+    // Principled parameters live in [0, 1]; colours and emission are
+    // non-negative. Outside that the lobe weights turn negative or NaN.
+    auto unit = [&](const char* key, float v) {
+        if (!(v >= 0.0f && v <= 1.0f)) throw JsonError("bsdf \"" + name + "\": " + key + " must lie in [0, 1]");
+    };
+    unit("metallic", b.m.metallic);
+    unit("roughness", b.m.roughness);
+    unit("specular", b.m.specular);
+    if (!(base.x >= 0.0f && base.y >= 0.0f && base.z >= 0.0f))
+        throw JsonError("bsdf \"" + name + "\": color must be non-negative");
+    if (!(b.emission.x >= 0.0f && b.emission.y >= 0.0f && b.emission.z >= 0.0f))
+        throw JsonError("bsdf \"" + name + "\": emission must be non-negative");
     return b;
 }
 
@@ -470,16 +482,23 @@ HostScene load_scene_json(const std::string& path, bool allow_missing) {
         const Json& pc = cam.obj[0].second;
         const Json& res = pc.at("res");
         if (!res.is_array() || res.arr.size() != 2) throw JsonError("camera res must be [w, h]");
-        int W = (int)res.arr[0].as_number(), H = (int)res.arr[1].as_number();
-        if (W <= 0 || H <= 0) throw JsonError("camera res must be positive");
+        const double wd = res.arr[0].as_number(), hd = res.arr[1].as_number();
+        // the same bound as aqua_scene_set_resolution
+        if (!(wd >= 1 && hd >= 1 && wd <= 16384 && hd <= 16384) || wd != std::floor(wd) || hd != std::floor(hd))
+            throw JsonError("camera res must be two integers in [1, 16384]");
+        const int W = (int)wd, H = (int)hd;
         double t[3] = {0, 0, 0}, r[3] = {0, 0, 0};
         if (const Json* tr = pc.find("transform")) {
             if (const Json* tt = tr->find("translate")) { v3 v = read3(*tt); t[0] = v.x; t[1] = v.y; t[2] = v.z; }
             if (const Json* rr = tr->find("rotate")) { v3 v = read3(*rr); r[0] = v.x; r[1] = v.y; r[2] = v.z; }
         }
-        s.cam = make_camera(W, H, (float)pc.at("fov").as_number(),
-                            pc.find("lens_radius") ? (float)pc.at("lens_radius").as_number() : 0.0f,
-                            pc.find("focal") ? (float)pc.at("focal").as_number() : 1.0f, t, r);
+        const double fov = pc.at("fov").as_number();
+        const double lens = pc.find("lens_radius") ? pc.at("lens_radius").as_number() : 0.0;
+        const double focal = pc.find("focal") ? pc.at("focal").as_number() : 1.0;
+        if (!(fov > 0 && fov < 180)) throw JsonError("camera fov must lie in (0, 180) degrees");
+        if (!(lens >= 0 && lens < 1e30) || !(focal > 0 && focal < 1e30))
+            throw JsonError("camera lens_radius must be >= 0 and focal > 0");
+        s.cam = make_camera(W, H, (float)fov, (float)lens, (float)focal, t, r);
         // lights (cbox.json:544-561)
         if (const Json* ls = root.find("lights")) {
             for (auto& l : ls->arr) {
@@ -610,12 +629,21 @@ void load_integrator_json(const std::string& path, aqua_integrator_cfg* cfg) {
         geti("batch_size", cfg->batch_size);
         geti("max_depth", cfg->max_depth);
         geti("training_iters", cfg->training_iters);
-        if (const Json* v = j.find("learning_rate")) cfg->learning_rate = (float)v->as_number();
+        if (const Json* v = j.find("learning_rate")) {
+            const double lr = v->as_number();
+            if (!(lr > 0.0) || lr > 3.0e38) throw JsonError("learning_rate must be a positive number");
+            cfg->learning_rate = (float)lr;
+        }
         if (const Json* v = j.find("visualize_cache")) {
             if (v->kind != Json::Bool) throw JsonError("visualize_cache must be a boolean");
             cfg->visualize_cache = v->b ? 1 : 0;
         }
-        if (const Json* v = j.find("seed")) cfg->seed = (uint64_t)v->as_number();
+        if (const Json* v = j.find("seed")) {
+            const double d = v->as_number();
+            if (d < 0 || d >= 18446744073709551616.0 || d != std::floor(d))
+                throw JsonError("seed must be a non-negative integer below 2^64");
+            cfg->seed = (uint64_t)d;
+        }
     } catch (JsonError& e) {
         throw SceneError(AQUA_ERR_PARSE, path + ": " + e.what());
     }

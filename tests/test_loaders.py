@@ -241,6 +241,31 @@ def test_non_finite_mesh_attributes_are_refused(host_ctx, tmp_path, field, bad):
     assert e.value.status == aqua.ERR_PARSE and "non-finite" in e.value.message
 
 
+@pytest.mark.parametrize("old,new", [('"res": [16, 12]', '"res": [1e20, 12]'), ('"res": [16, 12]', '"res": [16.5, 12]'),
+                                     ('"res": [16, 12]', '"res": [0, 12]'), ('"res": [16, 12]', '"res": [20000, 12]'),
+                                     ('"fov": 40.0', '"fov": 180.0'), ('"fov": 40.0', '"fov": -5'),
+                                     ('"focal": 1.0', '"focal": 0'), ('"lens_radius": 0.0', '"lens_radius": -1')])
+def test_bad_camera_is_refused(host_ctx, quad_scene, old, new):
+    d, p = quad_scene
+    text = p.read_text()
+    assert old in text
+    p.write_text(text.replace(old, new))
+    with pytest.raises(aqua.AquaError) as e:
+        host_ctx.load_scene(str(p))
+    assert e.value.status == aqua.ERR_PARSE and "camera" in e.value.message
+
+
+@pytest.mark.parametrize("over", [dict(metallic=1.5), dict(roughness=-0.1), dict(specular=2.0),
+                                  dict(emission=-1.0), dict(color={"Float3": [0.5, -0.2, 0.5]})])
+def test_out_of_range_material_is_refused(host_ctx, tmp_path, over):
+    write_mesh(tmp_path / "q.mesh", [[0, 0, 0], [1, 0, 0], [0, 1, 0]], [[0, 1, 2]])
+    p = tmp_path / "s.json"
+    p.write_text(json.dumps(scene_json([("q.mesh", "a")], {"a": principled(**over)})))
+    with pytest.raises(aqua.AquaError) as e:
+        host_ctx.load_scene(str(p))
+    assert e.value.status == aqua.ERR_PARSE and "bsdf" in e.value.message
+
+
 def test_out_of_range_json_number_is_refused(host_ctx, quad_scene):
     d, p = quad_scene
     p.write_text(p.read_text().replace('"fov": 40.0', '"fov": 1e999'))
@@ -278,6 +303,14 @@ def test_integrator_json(host_ctx, tmp_path):
     p.write_text(json.dumps({"type": "pt", "spp": -3}))
     with pytest.raises(aqua.AquaError):
         host_ctx.integrator(str(p))
+    for bad in ({"learning_rate": 0}, {"learning_rate": -1e-3}, {"seed": -1}, {"seed": 1.5},
+                {"seed": 2.0 ** 64}):
+        p.write_text(json.dumps(dict({"type": "nrc"}, **bad)))
+        with pytest.raises(aqua.AquaError) as e:
+            host_ctx.integrator(str(p))
+        assert e.value.status == aqua.ERR_PARSE, bad
+    p.write_text(json.dumps({"type": "pt", "seed": 2.0 ** 63}))
+    assert host_ctx.integrator(str(p)).seed == 2 ** 63
 
 
 # ---------------------------------------------------------------- reference files
