@@ -228,7 +228,9 @@ typedef struct aqua_batch_stats {
 AQUA_API aqua_status aqua_create(aqua_ctx** out, const aqua_options* opt);
 AQUA_API void aqua_destroy(aqua_ctx* ctx);
 /* Message of the last failing call on ctx ("" when none). Valid until the
- * next call on ctx. aqua_create failures are reported by aqua_last_error(NULL). */
+ * next call on ctx. aqua_create failures are reported by aqua_last_error(NULL).
+ * The text is UTF-8 (input bytes it quotes that are not are written as \xNN),
+ * at most 1024 bytes. */
 AQUA_API const char* aqua_last_error(const aqua_ctx* ctx);
 AQUA_API const char* aqua_status_string(aqua_status s);
 /* ABI version: 100 x major + minor. Major 2: aqua_scene_export_bvh returns
