@@ -71,7 +71,8 @@ class IntegratorCfg(C.Structure):
     _fields_ = [("type", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32), ("rr_depth", C.c_int32),
                 ("batch_size", C.c_int32), ("training_iters", C.c_int32), ("learning_rate", C.c_float),
                 ("visualize_cache", C.c_int32), ("seed", C.c_uint64), ("spp_offset", C.c_int32),
-                ("nrc_train_samples", C.c_int32), ("nrc_query_vertex", C.c_int32), ("reserved0", C.c_int32)]
+                ("nrc_train_samples", C.c_int32), ("nrc_query_vertex", C.c_int32), ("row_begin", C.c_int32),
+                ("row_step", C.c_int32), ("reserved0", C.c_int32)]
 
 
 class Tuning(C.Structure):
@@ -108,7 +109,10 @@ class Camera(C.Structure):
 
 class Material(C.Structure):
     _fields_ = [("base_color", C.c_float * 3), ("base_texture", C.c_int32), ("metallic", C.c_float),
-                ("roughness", C.c_float), ("specular", C.c_float), ("reserved", C.c_int32)]
+                ("roughness", C.c_float), ("specular", C.c_float), ("specular_tint", C.c_float),
+                ("sheen", C.c_float), ("sheen_tint", C.c_float), ("clearcoat", C.c_float),
+                ("clearcoat_roughness", C.c_float), ("transmission", C.c_float), ("ior", C.c_float),
+                ("reserved", C.c_int32 * 2)]
 
 
 class Light(C.Structure):

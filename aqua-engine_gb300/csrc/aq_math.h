@@ -307,24 +307,48 @@ AQ_HD v3 offset_ray(v3 p, v3 n) {
 }
 
 // ------------------------------------------------------------------ BSDF
-// Lambert + GGX subset of `Principled` (scenes/cbox.json:3-62): base color,
-// metallic, roughness, specular. Every other lobe is 0 in both reference
-// scenes. f = (1-m) C/pi + D G2 F / (4 cos_o cos_i), with
+// `Principled` (scenes/cbox.json:3-62). The base model is Lambert + GGX:
+// f = (1-m) C/pi + D G2 F / (4 cos_o cos_i), with
 //   D   GGX / Trowbridge-Reitz (Walter et al. 2007, EGSR),
 //   G2  height-correlated Smith, 1 / (1 + L(wo) + L(wi)),
 //   F   Schlick, F0 = lerp(0.08*specular, C, m),
 //   alpha = max(roughness^2, 1e-3).
-// When F0 = 0 (specular 0 and metallic 0, as every material of the reference
-// scenes has) there is no GGX lobe at all: the surface is Lambertian.
-// Sampling picks the GGX lobe with probability p_s and then samples visible
-// normals (Heitz 2018, "Sampling the GGX Distribution of Visible Normals",
-// JCGT 7(4)); otherwise cosine-weighted. The pdf is the mixture pdf.
+// When F0 = 0 (specular 0 and metallic 0) there is no GGX lobe at all: the
+// surface is Lambertian. Sampling picks the GGX lobe with probability p_s and
+// then samples visible normals (Heitz 2018, "Sampling the GGX Distribution
+// of Visible Normals", JCGT 7(4)); otherwise cosine-weighted. The pdf is the
+// mixture pdf.
+//
+// The full model (the `*_full` functions, used by scenes whose materials set
+// specular_tint, sheen, clearcoat or transmission) adds, with t =
+// transmission and C_t = C / lum(C):
+//   diffuse and sheen weighted by (1-m)(1-t); sheen = sheen *
+//     lerp(1, C_t, sheen_tint) * (1 - |wi.h|)^5 (Burley 2012);
+//   the Schlick lobe weighted by 1 - (1-m)t, its dielectric F0 tinted:
+//     0.08 * specular * lerp(1, C_t, specular_tint);
+//   a rough dielectric lobe weighted by (1-m)t (Walter et al. 2007): exact
+//     dielectric Fresnel F at the microfacet, reflection F D G2 / (4 cos cos)
+//     (white), refraction C (1-F) D G2 |wi.h||wo.h| / (|cos_i| cos_o (wo.h +
+//     eta wi.h)^2), eta = n(wi side) / n(wo side) = ior entering the front
+//     face, 1/ior leaving it; sampled by visible normals, then reflection
+//     with probability F;
+//   clearcoat: 0.25 clearcoat D_GTR1 F_Schlick(0.04) G1(wo) G1(wi) /
+//     (4 cos cos), GTR1 alpha = clearcoat_roughness^2, G1 with alpha 0.25
+//     (Burley 2012, sampled by its closed-form inverse).
+// With those four parameters 0 every full-model expression reduces to the
+// base model's arithmetic exactly (additions of 0, products with 1).
 struct Bsdf {
     v3 color;
     float metallic, alpha, specular;
     v3 F0;
     float p_spec;
     bool has_spec;
+    // full model only
+    float wdiff, wspec, wglass;  // (1-m)(1-t), 1-(1-m)t, (1-m)t
+    v3 sheen;                    // wdiff * sheen * lerp(1, C_t, sheen_tint)
+    float eta;                   // n(other side) / n(wo side)
+    float cc, cc_a2;             // 0.25 clearcoat, GTR1 alpha^2
+    float p_glass, p_cc;         // lobe-selection probabilities
 };
 AQ_HD Bsdf make_bsdf(v3 color, float metallic, float roughness, float specular) {
     Bsdf b;
@@ -340,6 +364,42 @@ AQ_HD Bsdf make_bsdf(v3 color, float metallic, float roughness, float specular) 
     float ps = (ws + wd) > 0.0f ? ws / (ws + wd) : 0.5f;
     if (ws > 0.0f && wd > 0.0f) ps = fminf_(fmaxf_(ps, 0.1f), 0.9f);
     b.p_spec = b.has_spec ? ps : 0.0f;
+    b.wdiff = 1.0f - metallic; b.wspec = 1.0f; b.wglass = 0.0f;
+    b.sheen = mk(0, 0, 0);
+    b.eta = 1.0f; b.cc = 0.0f; b.cc_a2 = 0.0f; b.p_glass = 0.0f; b.p_cc = 0.0f;
+    return b;
+}
+// front: wo lies on the side the triangle's winding normal points to.
+AQ_HD Bsdf make_bsdf_full(v3 color, float metallic, float roughness, float specular, float spec_tint, float sheen,
+                          float sheen_tint, float clearcoat, float cc_rough, float tr, float ior_in, bool front) {
+    Bsdf b;
+    b.color = color;
+    b.metallic = metallic;
+    b.alpha = fmaxf_(roughness * roughness, 1e-3f);
+    b.specular = specular;
+    const float lc = lum(color);
+    const v3 one = mk(1.0f, 1.0f, 1.0f);
+    const v3 tint = lc > 0.0f ? color * (1.0f / lc) : one;
+    v3 f0d = lerp(one, tint, spec_tint) * (0.08f * specular);
+    b.F0 = lerp(f0d, color, metallic);
+    b.wdiff = (1.0f - metallic) * (1.0f - tr);
+    b.wglass = (1.0f - metallic) * tr;
+    b.wspec = 1.0f - b.wglass;
+    b.has_spec = (b.F0.x + b.F0.y + b.F0.z) > 0.0f && b.wspec > 0.0f;
+    b.sheen = lerp(one, tint, sheen_tint) * (b.wdiff * sheen);
+    const float ior = fmaxf_(ior_in, 1.001f);
+    b.eta = front ? ior : 1.0f / ior;
+    b.cc = 0.25f * clearcoat;
+    const float ca = fminf_(fmaxf_(cc_rough * cc_rough, 1e-3f), 0.999f);
+    b.cc_a2 = ca * ca;
+    float ws = b.has_spec ? lum(b.F0) * b.wspec : 0.0f;
+    float wd = b.wdiff * lc + lum(b.sheen);
+    float ps = (ws + wd) > 0.0f ? ws / (ws + wd) : 0.5f;
+    if (ws > 0.0f && wd > 0.0f) ps = fminf_(fmaxf_(ps, 0.1f), 0.9f);
+    b.p_spec = b.has_spec ? ps : 0.0f;
+    const float tot = wd + ws + b.wglass + b.cc;
+    b.p_glass = b.wglass > 0.0f ? b.wglass / tot : 0.0f;
+    b.p_cc = b.cc > 0.0f ? b.cc / tot : 0.0f;
     return b;
 }
 AQ_HD float ggx_D(float a2, float cos_h) {
@@ -356,6 +416,21 @@ AQ_HD v3 schlick(v3 F0, float c) {
     float m = fminf_(fmaxf_(1.0f - c, 0.0f), 1.0f);
     float m5 = (m * m) * (m * m) * m;
     return F0 + (mk(1.0f, 1.0f, 1.0f) - F0) * m5;
+}
+AQ_HD float pow5_(float x) { return (x * x) * (x * x) * x; }
+// GTR1 (Berry) distribution of the clearcoat lobe (Burley 2012, appendix B).
+AQ_HD float gtr1_D(float a2, float cos_h) {
+    return (a2 - 1.0f) / (kPi * logf(a2) * (1.0f + (a2 - 1.0f) * cos_h * cos_h));
+}
+// Unpolarised dielectric Fresnel reflectance; cos_i >= 0 on the incident
+// side, eta = n(transmitted side) / n(incident side).
+AQ_HD float fresnel_dielectric(float cos_i, float eta) {
+    float s2 = (1.0f - cos_i * cos_i) / (eta * eta);
+    if (s2 >= 1.0f) return 1.0f;
+    float ct = sqrtf(1.0f - s2);
+    float rs = (cos_i - eta * ct) / (cos_i + eta * ct);
+    float rp = (eta * cos_i - ct) / (eta * cos_i + ct);
+    return 0.5f * (rs * rs + rp * rp);
 }
 // wo, wi in the local frame (z = normal). Returns f (not times cos).
 AQ_HD v3 bsdf_eval(const Bsdf& b, v3 wo, v3 wi) {
@@ -390,27 +465,156 @@ AQ_HD float bsdf_pdf(const Bsdf& b, v3 wo, v3 wi) {
     }
     return (1.0f - b.p_spec) * pd + b.p_spec * ps;
 }
+// GGX visible-normal sample for wo (Heitz 2018).
+AQ_HD v3 ggx_vndf(float a, v3 wo, float u1, float u2) {
+    v3 Vh = normalize(mk(a * wo.x, a * wo.y, wo.z));
+    float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
+    v3 T1 = lensq > 0.0f ? mk(-Vh.y, Vh.x, 0.0f) * (1.0f / sqrtf(lensq)) : mk(1.0f, 0.0f, 0.0f);
+    v3 T2 = cross(Vh, T1);
+    float r = sqrtf(u1);
+    float phi = 2.0f * kPi * u2;
+    float t1 = r * cosf(phi), t2 = r * sinf(phi);
+    float s = 0.5f * (1.0f + Vh.z);
+    t2 = (1.0f - s) * sqrtf(fmaxf_(1.0f - t1 * t1, 0.0f)) + s * t2;
+    v3 Nh = T1 * t1 + T2 * t2 + Vh * sqrtf(fmaxf_(0.0f, 1.0f - t1 * t1 - t2 * t2));
+    return normalize(mk(a * Nh.x, a * Nh.y, fmaxf_(0.0f, Nh.z)));
+}
 // Returns the sampled local direction; wi.z <= 0 means "no valid sample".
 AQ_HD v3 bsdf_sample(const Bsdf& b, v3 wo, float ulobe, float u1, float u2) {
     if (ulobe < b.p_spec) {
-        float a = b.alpha;
-        v3 Vh = normalize(mk(a * wo.x, a * wo.y, wo.z));
-        float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
-        v3 T1 = lensq > 0.0f ? mk(-Vh.y, Vh.x, 0.0f) * (1.0f / sqrtf(lensq)) : mk(1.0f, 0.0f, 0.0f);
-        v3 T2 = cross(Vh, T1);
-        float r = sqrtf(u1);
-        float phi = 2.0f * kPi * u2;
-        float t1 = r * cosf(phi), t2 = r * sinf(phi);
-        float s = 0.5f * (1.0f + Vh.z);
-        t2 = (1.0f - s) * sqrtf(fmaxf_(1.0f - t1 * t1, 0.0f)) + s * t2;
-        v3 Nh = T1 * t1 + T2 * t2 + Vh * sqrtf(fmaxf_(0.0f, 1.0f - t1 * t1 - t2 * t2));
-        v3 Ne = normalize(mk(a * Nh.x, a * Nh.y, fmaxf_(0.0f, Nh.z)));
+        v3 Ne = ggx_vndf(b.alpha, wo, u1, u2);
         float d = dot(wo, Ne);
         return Ne * (2.0f * d) - wo;
     }
     float r = sqrtf(u1);
     float phi = 2.0f * kPi * u2;
     return mk(r * cosf(phi), r * sinf(phi), sqrtf(fmaxf_(0.0f, 1.0f - u1)));
+}
+
+// Half vector of refraction between wo (this side) and wi (the other side,
+// index ratio eta), oriented to +z.
+AQ_HD v3 refraction_half(v3 wo, v3 wi, float eta) {
+    v3 h = normalize(wo + wi * eta);
+    return h.z < 0.0f ? -h : h;
+}
+AQ_HD v3 bsdf_eval_full(const Bsdf& b, v3 wo, v3 wi) {
+    if (wo.z <= 0.0f || wi.z == 0.0f) return mk(0, 0, 0);
+    const float a2 = b.alpha * b.alpha;
+    if (wi.z < 0.0f) {
+        if (!(b.wglass > 0.0f)) return mk(0, 0, 0);
+        v3 h = refraction_half(wo, wi, b.eta);
+        float co = dot(wo, h), ci = dot(wi, h);
+        if (!(co > 0.0f && ci < 0.0f)) return mk(0, 0, 0);
+        float F = fresnel_dielectric(co, b.eta);
+        float den = co + b.eta * ci;
+        float G2 = 1.0f / (1.0f + ggx_Lambda(a2, wo.z) + ggx_Lambda(a2, wi.z));
+        float v = b.wglass * (1.0f - F) * ggx_D(a2, h.z) * G2 * (-ci) * co / (-wi.z * wo.z * den * den);
+        return b.color * v;
+    }
+    v3 f = b.color * (b.wdiff * kInvPi);
+    v3 h = wo + wi;
+    float hl = length(h);
+    if (!(hl > 0.0f)) return f;
+    h = h * (1.0f / hl);
+    const float wih = dot(wi, h);
+    f = f + b.sheen * pow5_(fminf_(fmaxf_(1.0f - wih, 0.0f), 1.0f));
+    const float den = 4.0f * wo.z * wi.z;
+    if (b.has_spec || b.wglass > 0.0f) {
+        float D = ggx_D(a2, h.z);
+        float G2 = 1.0f / (1.0f + ggx_Lambda(a2, wo.z) + ggx_Lambda(a2, wi.z));
+        if (b.has_spec) {
+            v3 F = schlick(b.F0, wih);
+            f = f + F * (D * G2 / den * b.wspec);
+        }
+        if (b.wglass > 0.0f) {
+            float F = fresnel_dielectric(dot(wo, h), b.eta);
+            float v = b.wglass * F * D * G2 / den;
+            f = f + mk(v, v, v);
+        }
+    }
+    if (b.cc > 0.0f) {
+        const float ga2 = 0.0625f;  // alpha 0.25
+        float G = 1.0f / ((1.0f + ggx_Lambda(ga2, wo.z)) * (1.0f + ggx_Lambda(ga2, wi.z)));
+        float m = fminf_(fmaxf_(1.0f - wih, 0.0f), 1.0f);
+        float Fc = 0.04f + 0.96f * pow5_(m);
+        float v = b.cc * gtr1_D(b.cc_a2, h.z) * Fc * G / den;
+        f = f + mk(v, v, v);
+    }
+    return f;
+}
+AQ_HD float bsdf_pdf_full(const Bsdf& b, v3 wo, v3 wi) {
+    if (wo.z <= 0.0f || wi.z == 0.0f) return 0.0f;
+    const float a2 = b.alpha * b.alpha;
+    const float G1 = 1.0f / (1.0f + ggx_Lambda(a2, wo.z));
+    if (wi.z < 0.0f) {
+        if (!(b.p_glass > 0.0f)) return 0.0f;
+        v3 h = refraction_half(wo, wi, b.eta);
+        float co = dot(wo, h), ci = dot(wi, h);
+        if (!(co > 0.0f && ci < 0.0f)) return 0.0f;
+        float F = fresnel_dielectric(co, b.eta);
+        float den = co + b.eta * ci;
+        return b.p_glass * (1.0f - F) * G1 * ggx_D(a2, h.z) * co / wo.z * (b.eta * b.eta * (-ci) / (den * den));
+    }
+    float pd = wi.z * kInvPi;
+    float ps = 0.0f, pg = 0.0f, pc = 0.0f;
+    v3 h = wo + wi;
+    float hl = length(h);
+    if (hl > 0.0f) {
+        h = h * (1.0f / hl);
+        float pv = G1 * ggx_D(a2, h.z) / (4.0f * wo.z);
+        if (b.p_spec > 0.0f) ps = pv;
+        if (b.p_glass > 0.0f) pg = fresnel_dielectric(dot(wo, h), b.eta) * pv;
+        if (b.p_cc > 0.0f) pc = gtr1_D(b.cc_a2, h.z) * h.z / (4.0f * dot(wo, h));
+    }
+    float base = (1.0f - b.p_spec) * pd + b.p_spec * ps;
+    return (1.0f - b.p_glass - b.p_cc) * base + b.p_glass * pg + b.p_cc * pc;
+}
+// Returns the sampled local direction: wi.z > 0 reflection, wi.z < 0
+// refraction (glass lobe only), wi = 0 no sample. A reflection that lands
+// below the surface or a refraction that lands above it is no sample, so
+// that the pdf of every direction returned is bsdf_pdf_full's.
+AQ_HD v3 bsdf_sample_full(const Bsdf& b, v3 wo, float ulobe, float u1, float u2) {
+    const v3 none = mk(0.0f, 0.0f, 0.0f);
+    if (ulobe < b.p_glass) {
+        v3 h = ggx_vndf(b.alpha, wo, u1, u2);
+        float co = dot(wo, h);
+        float F = fresnel_dielectric(co, b.eta);
+        if (ulobe < b.p_glass * F) {
+            v3 r = h * (2.0f * co) - wo;
+            return r.z > 0.0f ? r : none;
+        }
+        float ie = 1.0f / b.eta;
+        float s2 = ie * ie * fmaxf_(0.0f, 1.0f - co * co);
+        float ct = sqrtf(fmaxf_(0.0f, 1.0f - s2));
+        v3 t = h * (ie * co - ct) - wo * ie;
+        return t.z < 0.0f ? t : none;
+    }
+    ulobe -= b.p_glass;
+    if (ulobe < b.p_cc) {
+        float c2 = (1.0f - powf(b.cc_a2, 1.0f - u1)) / (1.0f - b.cc_a2);
+        float ch = sqrtf(fminf_(fmaxf_(c2, 0.0f), 1.0f));
+        float sh = sqrtf(fmaxf_(0.0f, 1.0f - ch * ch));
+        float phi = 2.0f * kPi * u2;
+        v3 h = mk(sh * cosf(phi), sh * sinf(phi), ch);
+        float d = dot(wo, h);
+        if (d < 0.0f) { h = -h; d = -d; }
+        v3 r = h * (2.0f * d) - wo;
+        return r.z > 0.0f ? r : none;
+    }
+    ulobe -= b.p_cc;
+    const float rest = 1.0f - b.p_glass - b.p_cc;
+    v3 r = bsdf_sample(b, wo, rest > 0.0f ? ulobe / rest : 1.0f, u1, u2);
+    return r.z > 0.0f ? r : none;
+}
+
+// The base or the full model, chosen at compile time by the kernels.
+template <bool FULL>
+AQ_HD v3 bsdf_eval_t(const Bsdf& b, v3 wo, v3 wi) { return FULL ? bsdf_eval_full(b, wo, wi) : bsdf_eval(b, wo, wi); }
+template <bool FULL>
+AQ_HD float bsdf_pdf_t(const Bsdf& b, v3 wo, v3 wi) { return FULL ? bsdf_pdf_full(b, wo, wi) : bsdf_pdf(b, wo, wi); }
+template <bool FULL>
+AQ_HD v3 bsdf_sample_t(const Bsdf& b, v3 wo, float ul, float u1, float u2) {
+    return FULL ? bsdf_sample_full(b, wo, ul, u1, u2) : bsdf_sample(b, wo, ul, u1, u2);
 }
 
 AQ_HD float power_heuristic(float a, float b) {

@@ -45,6 +45,7 @@ __device__ __forceinline__ unsigned long long device_clock_ns() {
 // says whether the path goes on with the extension ray (o, dir) afterwards.
 struct LanePath {
     v3 o, dir, thr;
+    v3 so;  // shadow-ray origin when it differs from o (full model: glass)
     float pdf_b;
     int depth;
     uint64_t st, inc;
@@ -68,14 +69,16 @@ __device__ __forceinline__ void start_sample(const DevJob& J, uint32_t pixel, ui
 
 // BSDF sampling and Russian roulette at shading point p: the next extension
 // ray, or false when the path ends.
+template <bool FULL>
 __device__ __forceinline__ bool continue_path(const Bsdf& B, v3 wol, const float* u, v3 T, v3 Bt, v3 ns, v3 ng,
                                               v3 p, bool smooth, int rr_depth, LanePath& P) {
-    v3 wil = bsdf_sample(B, wol, u[3], u[4], u[5]);
-    if (!(wil.z > 0.0f && wol.z > 0.0f)) return false;
-    float pdf = bsdf_pdf(B, wol, wil);
-    v3 f = bsdf_eval(B, wol, wil);
+    v3 wil = bsdf_sample_t<FULL>(B, wol, u[3], u[4], u[5]);
+    const bool through = FULL && wil.z < 0.0f;  // refracted by the glass lobe
+    if (!((wil.z > 0.0f || through) && wol.z > 0.0f)) return false;
+    float pdf = bsdf_pdf_t<FULL>(B, wol, wil);
+    v3 f = bsdf_eval_t<FULL>(B, wol, wil);
     if (!(pdf > 0.0f)) return false;
-    v3 thr = P.thr * f * (wil.z / pdf);
+    v3 thr = P.thr * f * ((FULL ? fabsf(wil.z) : wil.z) / pdf);
     bool ok = maxc(thr) > 0.0f && isfinite(thr.x) && isfinite(thr.y) && isfinite(thr.z);
     if (ok && P.depth >= rr_depth) {
         float q = fminf(1.0f, maxc(thr));
@@ -84,10 +87,14 @@ __device__ __forceinline__ bool continue_path(const Bsdf& B, v3 wol, const float
     }
     if (!ok) return false;
     const v3 dir = normalize(T * wil.x + Bt * wil.y + ns * wil.z);
-    if (smooth && !(dot(dir, ng) > 0.0f)) return false;  // below the geometric surface
+    if (through) {
+        if (!(dot(dir, ng) < 0.0f)) return false;  // refraction must cross the surface
+    } else if (smooth && !(dot(dir, ng) > 0.0f)) {
+        return false;  // below the geometric surface
+    }
     P.thr = thr;
     P.dir = dir;
-    P.o = offset_ray(p, ng);
+    P.o = offset_ray(p, through ? -ng : ng);
     P.pdf_b = pdf;
     P.depth = P.depth + 1;
     return true;
@@ -98,6 +105,7 @@ __device__ __forceinline__ bool continue_path(const Bsdf& B, v3 wol, const float
 // and Russian roulette. Contributions are added to `sum` in the wavefront's
 // order (the light sample's once its shadow ray is traced). Returns false
 // when the path ends (a scheduled shadow ray is still traced).
+template <bool FULL>
 __device__ __forceinline__ bool shade_hit(const DevScene& S, int max_depth, int rr_depth, const float* lut,
                                           const TraceResult& h, LanePath& P, v3& sum) {
     const v3 thr = P.thr;
@@ -129,7 +137,8 @@ __device__ __forceinline__ bool shade_hit(const DevScene& S, int max_depth, int 
         }
     }
     if (depth >= max_depth) return false;
-    if (dot(ng, wo) < 0.0f) ng = -ng;
+    const bool front = dot(ng, wo) >= 0.0f;  // wo on the winding normal's side
+    if (!front) ng = -ng;
     const v3 ns = shading_normal(S, h.tri, h.u, h.v, ng, wo);
     DevMaterial m = S.mats[info & 0xffffu];
     v3 base = f3(m.a);
@@ -142,7 +151,14 @@ __device__ __forceinline__ bool shade_hit(const DevScene& S, int max_depth, int 
         float tv = t0.y * w0 + t1.y * h.u + t2.y * h.v;
         base = base * tex_bilinear(S, ti, tu, tv, lut);
     }
-    Bsdf B = make_bsdf(base, m.b.x, m.b.y, m.b.z);
+    Bsdf B;
+    if (FULL) {
+        const float4* xp = S.mext + 2 * (size_t)(info & 0xffffu);
+        const float4 x0 = ldg_(xp), x1 = ldg_(xp + 1);
+        B = make_bsdf_full(base, m.b.x, m.b.y, m.b.z, x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, front);
+    } else {
+        B = make_bsdf(base, m.b.x, m.b.y, m.b.z);
+    }
     v3 T, Bt;
     onb(ns, T, Bt);
     v3 wol = mk(dot(wo, T), dot(wo, Bt), dot(wo, ns));
@@ -155,15 +171,17 @@ __device__ __forceinline__ bool shade_hit(const DevScene& S, int max_depth, int 
         float pmf = L.e2.w;
         v3 contrib = mk(0, 0, 0), wi;
         float dist = 0.0f;
+        bool below = false;  // light sample on the far side (glass lobe)
         if (ty == AQUA_LIGHT_POINT) {
             v3 dl = f3(L.p0) - p;
             float d2 = dot(dl, dl);
             dist = sqrtf(d2);
             wi = dl * (1.0f / dist);
             float cs = dot(wi, ns), cg = dot(wi, ng);
-            if (cs > 0.0f && cg > 0.0f && d2 > 0.0f) {
+            below = FULL && B.wglass > 0.0f && cs < 0.0f && cg < 0.0f;
+            if (((cs > 0.0f && cg > 0.0f) || below) && d2 > 0.0f) {
                 v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
-                contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs / (d2 * pmf));
+                contrib = thr * bsdf_eval_t<FULL>(B, wol, wil) * f3(L.le) * ((FULL ? fabsf(cs) : cs) / (d2 * pmf));
             }
         } else {
             v3 le1 = f3(L.e1), le2 = f3(L.e2), xl;
@@ -179,25 +197,27 @@ __device__ __forceinline__ bool shade_hit(const DevScene& S, int max_depth, int 
             dist = sqrtf(d2);
             wi = dl * (1.0f / dist);
             float cl = -dot(wi, nl), cs = dot(wi, ns), cg = dot(wi, ng);
-            if (cl > 0.0f && cs > 0.0f && cg > 0.0f && d2 > 0.0f) {
+            below = FULL && B.wglass > 0.0f && cs < 0.0f && cg < 0.0f;
+            if (cl > 0.0f && ((cs > 0.0f && cg > 0.0f) || below) && d2 > 0.0f) {
                 v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
                 float pl = pmf * d2 / (L.e1.w * cl);
-                float pb = bsdf_pdf(B, wol, wil);
+                float pb = bsdf_pdf_t<FULL>(B, wol, wil);
                 float w = power_heuristic(pl, pb);
-                contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs * w / pl);
+                contrib = thr * bsdf_eval_t<FULL>(B, wol, wil) * f3(L.le) * ((FULL ? fabsf(cs) : cs) * w / pl);
             }
         }
         if (contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f) {
-            // The shadow ray leaves from the same offset point as the
-            // extension ray.
+            // The shadow ray leaves from the offset point on the light's
+            // side; the extension ray sets its own origin afterwards.
             P.shadow = true;
             P.o = offset_ray(p, ng);
+            if (FULL) P.so = offset_ray(p, below ? -ng : ng);
             P.sdir = wi;
             P.stmax = dist * (1.0f - 1e-4f);
             P.contrib = contrib;
         }
     }
-    const bool alive = continue_path(B, wol, u, T, Bt, ns, ng, p, S.nrm != nullptr, rr_depth, P);
+    const bool alive = continue_path<FULL>(B, wol, u, T, Bt, ns, ng, p, S.nrm != nullptr, rr_depth, P);
     P.alive = alive;
     return alive;
 }
@@ -208,6 +228,7 @@ __device__ __forceinline__ bool shade_hit(const DevScene& S, int max_depth, int 
 // 4 resident blocks of 256 (64 registers): the spilled path state costs less
 // than the latency the extra warps hide (measured on the 64-job batch: 48,
 // 64 and 80 registers and the compiler's own 107 compared).
+template <bool FULL>
 __global__ void __launch_bounds__(256, 4) k_batch(const DevScene* __restrict__ scenes, const DevJob* __restrict__ jobs, int njobs,
                         uint32_t total_pixels, uint32_t* __restrict__ counters,
                         unsigned long long* __restrict__ clocks, unsigned long long* __restrict__ stats) {
@@ -262,14 +283,15 @@ __global__ void __launch_bounds__(256, 4) k_batch(const DevScene* __restrict__ s
         const bool any = P.shadow;
         if (any) ++n_sh;
         else ++n_ext;
-        const TraceResult h = traverse_fast(S, P.o, any ? P.sdir : P.dir, 0.0f, any ? P.stmax : INFINITY, any);
+        const TraceResult h = traverse_fast(S, (FULL && any) ? P.so : P.o, any ? P.sdir : P.dir, 0.0f,
+                                            any ? P.stmax : INFINITY, any);
         bool alive;
         if (any) {
             if (h.tri < 0) sum = sum + P.contrib;
             P.shadow = false;
             alive = P.alive;
         } else {
-            alive = shade_hit(S, J.max_depth, J.rr_depth, lut, h, P, sum);
+            alive = shade_hit<FULL>(S, J.max_depth, J.rr_depth, lut, h, P, sum);
             if (P.shadow) continue;
         }
         if (alive) continue;
@@ -334,9 +356,12 @@ static BatchResult launch_jobs(aqua_ctx* ctx, std::vector<DevJob>& jobs, std::ve
     const size_t n = jobs.size();
     int block = tune.block_trace > 0 ? tune.block_trace : 128;
     if (block != 64 && block != 128 && block != 256) throw Error(AQUA_ERR_INVALID_ARG, "block size must be 64, 128 or 256");
+    bool full = false;  // some scene's materials set the full model's lobes
+    for (const DevScene& sc : scenes) full = full || sc.mext != nullptr;
+    auto kernel = full ? k_batch<true> : k_batch<false>;
     int per_sm = tune.blocks_per_sm;
     if (per_sm <= 0) {
-        AQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, block, 0));
+        AQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0));
         per_sm = std::max(per_sm, 1);
     }
     int grid = ctx->num_sms * per_sm;
@@ -368,8 +393,8 @@ static BatchResult launch_jobs(aqua_ctx* ctx, std::vector<DevJob>& jobs, std::ve
             AQ_CUDA(cudaMemsetAsync(g.d_counters, 0, 4 * (n + 1), s));
             AQ_CUDA(cudaMemsetAsync(g.d_clocks, 0, 8 * (n + 1), s));
             AQ_CUDA(cudaMemsetAsync(g.d_stats, 0, 8 * 4, s));
-            k_batch<<<grid, block, 0, s>>>(g.d_scenes, g.d_jobs, (int)n, total_pixels, g.d_counters, g.d_clocks,
-                                            g.d_stats);
+            kernel<<<grid, block, 0, s>>>(g.d_scenes, g.d_jobs, (int)n, total_pixels, g.d_counters, g.d_clocks,
+                                           g.d_stats);
             AQ_CUDA(cudaGetLastError());
         };
         if (tune.use_graph != 0) {
@@ -394,8 +419,8 @@ static BatchResult launch_jobs(aqua_ctx* ctx, std::vector<DevJob>& jobs, std::ve
         AQ_CUDA(cudaMemsetAsync(g.d_counters, 0, 4 * (n + 1), st));
         AQ_CUDA(cudaMemsetAsync(g.d_clocks, 0, 8 * (n + 1), st));
         AQ_CUDA(cudaMemsetAsync(g.d_stats, 0, 8 * 4, st));
-        k_batch<<<grid, block, 0, st>>>(g.d_scenes, g.d_jobs, (int)n, total_pixels, g.d_counters, g.d_clocks,
-                                         g.d_stats);
+        kernel<<<grid, block, 0, st>>>(g.d_scenes, g.d_jobs, (int)n, total_pixels, g.d_counters, g.d_clocks,
+                                        g.d_stats);
         AQ_CUDA(cudaGetLastError());
     }
     AQ_CUDA(cudaEventRecord(ev.e[1], st));
@@ -485,8 +510,8 @@ void render_batch(aqua_ctx* ctx, const aqua_job* in, size_t n, const aqua_tuning
 
 void render_persistent(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, const aqua_tuning& tune,
                        float* rgb_out, uint32_t flags, aqua_stats* stats) {
-    if (cfg.spp <= 0 || cfg.max_depth < 0 || cfg.max_depth > 250)
-        throw Error(AQUA_ERR_INVALID_ARG, "spp must be > 0 and max_depth in [0, 250]");
+    if (cfg.spp <= 0) throw Error(AQUA_ERR_INVALID_ARG, "spp must be positive");
+    check_depths(cfg.max_depth, cfg.rr_depth);
     const aqua_camera& cam = sc->host.cam;
     const size_t pixels = (size_t)cam.width * (size_t)cam.height;
     if (pixels == 0 || pixels > 0xFFFFFF00ull) throw Error(AQUA_ERR_INVALID_ARG, "image size out of range");

@@ -89,7 +89,11 @@ void scene_build_device(aqua_ctx* ctx, aqua_scene* s) {
            o_mats = align256(o_uvs + 24 * nt), o_lights = align256(o_mats + 32 * h.mats.size()),
            o_texs = align256(o_lights + 64 * h.lights.size()),
            o_texels = align256(o_texs + 16 * h.textures.size()), o_nrm = align256(o_texels + 4 * texels),
-           total = align256(o_nrm + (h.nrm.empty() ? 0 : 48 * nt));
+           o_mext = align256(o_nrm + (h.nrm.empty() ? 0 : 48 * nt));
+    bool full_bsdf = false;
+    for (const aqua_material& m : h.mats)
+        if (m.specular_tint > 0.0f || m.sheen > 0.0f || m.clearcoat > 0.0f || m.transmission > 0.0f) full_bsdf = true;
+    size_t total = align256(o_mext + (full_bsdf ? 32 * h.mats.size() : 0));
     free_staging(s);
     if (ctx->host_only) {
         s->pinned = malloc(total);
@@ -127,6 +131,14 @@ void scene_build_device(aqua_ctx* ctx, aqua_scene* s) {
         memcpy(&tf, &tex, 4);
         mw[i].a = make_float4(m.base_color[0], m.base_color[1], m.base_color[2], tf);
         mw[i].b = make_float4(m.metallic, m.roughness, m.specular, 0.0f);
+    }
+    if (full_bsdf) {
+        float4* xw = (float4*)(p + o_mext);
+        for (size_t i = 0; i < h.mats.size(); ++i) {
+            const aqua_material& m = h.mats[i];
+            xw[2 * i] = make_float4(m.specular_tint, m.sheen, m.sheen_tint, m.clearcoat);
+            xw[2 * i + 1] = make_float4(m.clearcoat_roughness, m.transmission, m.ior, 0.0f);
+        }
     }
     DevLight* lw = (DevLight*)(p + o_lights);
     double cdf = 0.0;
@@ -167,6 +179,7 @@ void scene_build_device(aqua_ctx* ctx, aqua_scene* s) {
     ds.texs = (const DevTexture*)(d + o_texs);
     ds.texels = (const uint32_t*)(d + o_texels);
     ds.nrm = h.nrm.empty() ? nullptr : (const float4*)(d + o_nrm);
+    ds.mext = full_bsdf ? (const float4*)(d + o_mext) : nullptr;
     ds.n_nodes = (int32_t)nn;
     ds.n_tris = (int32_t)nt;
     ds.n_mats = (int32_t)h.mats.size();
@@ -576,7 +589,8 @@ AQUA_API aqua_status aqua_render(aqua_ctx* ctx, aqua_scene* s, const aqua_integr
         need(t.kernel == AQUA_KERNEL_WAVEFRONT || t.kernel == AQUA_KERNEL_PERSISTENT,
              "tuning.kernel must be an AQUA_KERNEL_* value");
         const uint32_t wavefront_only = AQUA_RENDER_COUNT | AQUA_RENDER_STAGE_TIMING | AQUA_RENDER_ACCUMULATE;
-        if (t.kernel == AQUA_KERNEL_PERSISTENT && !(flags & wavefront_only) && cfg->spp_offset == 0)
+        if (t.kernel == AQUA_KERNEL_PERSISTENT && !(flags & wavefront_only) && cfg->spp_offset == 0 &&
+            cfg->row_step <= 1)
             render_persistent(ctx, s, *cfg, t, rgb_out, flags, stats);
         else
             render_path(ctx, s, *cfg, t, rgb_out, flags, stats);
@@ -594,6 +608,7 @@ AQUA_API aqua_status aqua_autotune(aqua_ctx* ctx, aqua_scene* s, const aqua_inte
             throw Error(AQUA_ERR_UNSUPPORTED, "the autotuner tunes the path integrator");
         aqua_integrator_cfg c = *cfg;
         c.spp = std::max(1, std::min(cfg->spp, 16));
+        c.row_begin = c.row_step = 0;  // tuned on the whole image
         size_t pixels = (size_t)s->host.cam.width * (size_t)s->host.cam.height;
         DevBuf film;
         dev_alloc(ctx, film, 12 * pixels);

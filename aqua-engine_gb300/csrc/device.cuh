@@ -40,6 +40,10 @@ struct DevScene {
     const DevTexture* __restrict__ texs;
     const uint32_t* __restrict__ texels;  // RGBA8, sRGB
     const float4* __restrict__ nrm;    // 3 vertex normals per triangle (xyz, 0), leaf order; null = flat
+    // 2 words per material: (specular_tint, sheen, sheen_tint, clearcoat),
+    // (clearcoat_roughness, transmission, ior, 0); null when no material
+    // sets any of those lobes (the base-model kernels run then).
+    const float4* __restrict__ mext;
     int32_t n_nodes, n_tris, n_mats, n_lights, n_texs;
     float env[3];
     DevCamera cam;

@@ -22,6 +22,15 @@ struct Error : std::runtime_error {
     Error(aqua_status s, const std::string& m) : std::runtime_error(m), status(s) {}
 };
 
+// Depth limits shared by every render entry point. A path's depth lives in
+// the low 8 bits of its state word (one more than max_depth is stored after
+// the last bounce), so max_depth stays at or below 250; rr_depth is a bounce
+// index in the same range (a value above max_depth turns roulette off).
+inline void check_depths(int32_t max_depth, int32_t rr_depth) {
+    if (max_depth < 0 || max_depth > 250) throw Error(AQUA_ERR_INVALID_ARG, "max_depth must be in [0, 250]");
+    if (rr_depth < 0 || rr_depth > 250) throw Error(AQUA_ERR_INVALID_ARG, "rr_depth must be in [0, 250]");
+}
+
 #define AQ_CUDA(call)                                                                          \
     do {                                                                                       \
         cudaError_t e_ = (call);                                                               \

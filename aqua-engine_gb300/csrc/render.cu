@@ -44,6 +44,9 @@ struct WaveParams {
     // slot s = r * pixels + p runs samples r, r + K, r + 2K, ... of pixel p
     // into film copy r; the copies are summed in order r = 0..K-1.
     uint32_t replicas;
+    // Row subset (row_step > 1): film pixel p is image pixel
+    // (row_begin + (p / width) * row_step) * width + p % width.
+    uint32_t row_begin, row_step, width;
 };
 
 struct WavePtrs {
@@ -88,8 +91,16 @@ __device__ __forceinline__ uint32_t slot_work(const WaveParams& P, uint32_t s) {
     return npix * (uint32_t)P.spp;
 }
 
-// Pixel (the RNG stream), sample index and film entry of work item j of
-// slot s.
+// Image pixel of film pixel p (they differ for row-subset renders); the
+// image pixel names the camera ray and the random-number stream.
+__device__ __forceinline__ uint32_t image_pixel(const WaveParams& P, uint32_t p) {
+    if (P.row_step <= 1) return p;
+    uint32_t r = p / P.width;
+    return (P.row_begin + r * P.row_step) * P.width + (p - r * P.width);
+}
+
+// Pixel (the film pixel of the stream), sample index and film entry of
+// work item j of slot s.
 struct PathId {
     uint32_t pixel, sample, film;
 };
@@ -117,7 +128,7 @@ __device__ __forceinline__ bool start_path(const DevScene& S, const WaveParams& 
                                            uint32_t s, uint32_t j) {
     if (j >= slot_work(P, s)) return false;
     PathId pid = path_id(P, s, j);
-    uint32_t pixel = pid.pixel, sample = pid.sample;
+    uint32_t pixel = image_pixel(P, pid.pixel), sample = pid.sample;
     uint64_t st = path_rng_state(P.seed, pixel, sample), inc = pixel_inc(pixel);
     float u0 = draw(st, inc), u1 = draw(st, inc), u2 = draw(st, inc), u3 = draw(st, inc);
     v3 o, d;
@@ -256,7 +267,7 @@ __global__ void __launch_bounds__(128) k_trace_ext(DevScene S, WaveParams P, Wav
 // on and record every bounce (raw features, throughput, radiance gathered
 // so far) so that the radiance leaving each of their vertices becomes a
 // training target once the path is complete.
-template <bool SORTED, bool NRC = false>
+template <bool SORTED, bool NRC = false, bool FULL = false>
 __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, WavePtrs W, uint32_t cnt_in,
                                                uint32_t cnt_out) {
     __shared__ float lut[256];
@@ -311,7 +322,7 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
         const uint32_t train_id = (tag >> 8) - 1u;  // valid when tag != 0
         const PathId pid = path_id(P, s, j);
         const uint32_t pixel = pid.film;  // film entry owned by this slot
-        uint64_t st = (uint64_t)ps.x | ((uint64_t)ps.y << 32), inc = pixel_inc(pid.pixel);
+        uint64_t st = (uint64_t)ps.x | ((uint64_t)ps.y << 32), inc = pixel_inc(image_pixel(P, pid.pixel));
         v3 thr = f3(tpv);
         float pdf_b = tpv.w;
         int32_t tri = __float_as_int(h.w);
@@ -349,7 +360,8 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
             // the path the cache replaces.
             const int depth_limit = (NRC && tag) ? P.train_depth : P.max_depth;
             if ((int)depth < depth_limit) {
-                if (dot(ng, wo) < 0.0f) ng = -ng;
+                const bool front = dot(ng, wo) >= 0.0f;  // wo on the winding normal's side
+                if (!front) ng = -ng;
                 const v3 ns = shading_normal(S, tri, h.y, h.z, ng, wo);
                 DevMaterial m;
                 if (SORTED) {
@@ -368,7 +380,14 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                     float tv = t0.y * w0 + t1.y * h.y + t2.y * h.z;
                     base = base * tex_bilinear(S, ti, tu, tv, lut);
                 }
-                Bsdf B = make_bsdf(base, m.b.x, m.b.y, m.b.z);
+                Bsdf B;
+                if (FULL) {
+                    const float4* xp = S.mext + 2 * (size_t)(info & 0xffffu);
+                    const float4 x0 = ldg_(xp), x1 = ldg_(xp + 1);
+                    B = make_bsdf_full(base, m.b.x, m.b.y, m.b.z, x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, front);
+                } else {
+                    B = make_bsdf(base, m.b.x, m.b.y, m.b.z);
+                }
                 bool queried = false;
                 if (NRC) {
                     v3 kd = base * (1.0f - m.b.x);
@@ -408,15 +427,18 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                     float pmf = L.e2.w;
                     v3 contrib = mk(0, 0, 0), wi;
                     float dist = 0.0f;
+                    bool below = false;  // light sample on the far side (glass lobe)
                     if (ty == AQUA_LIGHT_POINT) {
                         v3 dl = f3(L.p0) - p;
                         float d2 = dot(dl, dl);
                         dist = sqrtf(d2);
                         wi = dl * (1.0f / dist);
                         float cs = dot(wi, ns), cg = dot(wi, ng);
-                        if (cs > 0.0f && cg > 0.0f && d2 > 0.0f) {
+                        below = FULL && B.wglass > 0.0f && cs < 0.0f && cg < 0.0f;
+                        if (((cs > 0.0f && cg > 0.0f) || below) && d2 > 0.0f) {
                             v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
-                            contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs / (d2 * pmf));
+                            contrib = thr * bsdf_eval_t<FULL>(B, wol, wil) * f3(L.le) *
+                                      ((FULL ? fabsf(cs) : cs) / (d2 * pmf));
                         }
                     } else {
                         v3 le1 = f3(L.e1), le2 = f3(L.e2), xl;
@@ -432,17 +454,19 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                         dist = sqrtf(d2);
                         wi = dl * (1.0f / dist);
                         float cl = -dot(wi, nl), cs = dot(wi, ns), cg = dot(wi, ng);
-                        if (cl > 0.0f && cs > 0.0f && cg > 0.0f && d2 > 0.0f) {
+                        below = FULL && B.wglass > 0.0f && cs < 0.0f && cg < 0.0f;
+                        if (cl > 0.0f && ((cs > 0.0f && cg > 0.0f) || below) && d2 > 0.0f) {
                             v3 wil = mk(dot(wi, T), dot(wi, Bt), cs);
                             float pl = pmf * d2 / (L.e1.w * cl);
-                            float pb = bsdf_pdf(B, wol, wil);
+                            float pb = bsdf_pdf_t<FULL>(B, wol, wil);
                             float w = power_heuristic(pl, pb);
-                            contrib = thr * bsdf_eval(B, wol, wil) * f3(L.le) * (cs * w / pl);
+                            contrib = thr * bsdf_eval_t<FULL>(B, wol, wil) * f3(L.le) *
+                                      ((FULL ? fabsf(cs) : cs) * w / pl);
                         }
                     }
                     if (contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f) {
                         uint32_t k = warp_append(&W.counters[kCntShadow], true);
-                        v3 so = offset_ray(p, ng);
+                        v3 so = offset_ray(p, below ? -ng : ng);
                         W.sh_o[k] = make_float4(so.x, so.y, so.z, __int_as_float((int)pixel));
                         W.sh_d[k] = make_float4(wi.x, wi.y, wi.z, dist * (1.0f - 1e-4f));
                         W.sh_c[k] = make_float4(contrib.x, contrib.y, contrib.z,
@@ -450,12 +474,13 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                     }
                 }
                 // BSDF sampling.
-                v3 wil = bsdf_sample(B, wol, u[3], u[4], u[5]);
-                if (!queried && wil.z > 0.0f && wol.z > 0.0f) {
-                    float pdf = bsdf_pdf(B, wol, wil);
-                    v3 f = bsdf_eval(B, wol, wil);
+                v3 wil = bsdf_sample_t<FULL>(B, wol, u[3], u[4], u[5]);
+                const bool through = FULL && wil.z < 0.0f;  // refracted by the glass lobe
+                if (!queried && (wil.z > 0.0f || through) && wol.z > 0.0f) {
+                    float pdf = bsdf_pdf_t<FULL>(B, wol, wil);
+                    v3 f = bsdf_eval_t<FULL>(B, wol, wil);
                     if (pdf > 0.0f) {
-                        thr = thr * f * (wil.z / pdf);
+                        thr = thr * f * ((FULL ? fabsf(wil.z) : wil.z) / pdf);
                         bool ok = maxc(thr) > 0.0f && isfinite(thr.x) && isfinite(thr.y) && isfinite(thr.z);
                         if (ok && (int)depth >= P.rr_depth) {
                             float q = fminf(1.0f, maxc(thr));
@@ -463,9 +488,13 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                             else thr = thr * (1.0f / q);
                         }
                         v3 wi = normalize(T * wil.x + Bt * wil.y + ns * wil.z);
-                        if (S.nrm && !(dot(wi, ng) > 0.0f)) ok = false;  // below the geometric surface
+                        if (through) {
+                            if (!(dot(wi, ng) < 0.0f)) ok = false;  // refraction must cross the surface
+                        } else if (S.nrm && !(dot(wi, ng) > 0.0f)) {
+                            ok = false;  // below the geometric surface
+                        }
                         if (ok) {
-                            v3 no = offset_ray(p, ng);
+                            v3 no = offset_ray(p, through ? -ng : ng);
                             W.ray_o[s] = make_float4(no.x, no.y, no.z, 0.0f);
                             W.ray_d[s] = make_float4(wi.x, wi.y, wi.z, INFINITY);
                             W.tp[s] = make_float4(thr.x, thr.y, thr.z, pdf);
@@ -681,12 +710,33 @@ SlotPlan plan_slots(size_t pixels, int spp, const aqua_tuning& tune) {
 }
 }  // namespace
 
+// Rows of the camera image a render covers (aqua_integrator_cfg row subset);
+// sets the parameters' row fields and returns the film's pixel count.
+static size_t plan_rows(const aqua_integrator_cfg& cfg, const DevCamera& cam, WaveParams& P) {
+    const size_t w = (size_t)cam.width, h = (size_t)cam.height;
+    size_t rows = h;
+    P.row_begin = 0;
+    P.row_step = 1;
+    P.width = (uint32_t)w;
+    if (cfg.row_step > 1) {
+        if (cfg.row_begin < 0 || cfg.row_begin >= cfg.row_step || (size_t)cfg.row_begin >= h)
+            throw Error(AQUA_ERR_INVALID_ARG, "row_begin must lie in [0, row_step) and below the image height");
+        rows = (h - (size_t)cfg.row_begin + (size_t)cfg.row_step - 1) / (size_t)cfg.row_step;
+        P.row_begin = (uint32_t)cfg.row_begin;
+        P.row_step = (uint32_t)cfg.row_step;
+    } else if (cfg.row_begin != 0 || cfg.row_step < 0) {
+        throw Error(AQUA_ERR_INVALID_ARG, "row_begin must be 0 and row_step >= 0 for whole images");
+    }
+    return w * rows;
+}
+
 void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, const aqua_tuning& tune,
                  float* rgb_out, uint32_t flags, aqua_stats* stats) {
     const DevScene& S = sc->ds;
     if (cfg.spp <= 0) throw Error(AQUA_ERR_INVALID_ARG, "spp must be positive");
-    if (cfg.max_depth < 0 || cfg.max_depth > 250) throw Error(AQUA_ERR_INVALID_ARG, "max_depth must be in [0, 250]");
-    size_t pixels = (size_t)S.cam.width * (size_t)S.cam.height;
+    check_depths(cfg.max_depth, cfg.rr_depth);
+    WaveParams P{};
+    size_t pixels = plan_rows(cfg, S.cam, P);
     if (pixels == 0 || pixels > (1u << 27)) throw Error(AQUA_ERR_INVALID_ARG, "resolution out of range");
     const SlotPlan plan = plan_slots(pixels, cfg.spp, tune);
     const size_t slots = plan.slots;
@@ -696,7 +746,6 @@ void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, 
     Workspace& w = ctx->ws;
     cudaStream_t st = ctx->stream;
 
-    WaveParams P{};
     P.replicas = plan.replicas;
     P.seed = cfg.seed;
     P.spp = cfg.spp;
@@ -720,7 +769,9 @@ void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, 
 
     auto trace_k = sorted ? (count ? k_trace_ext<true, true> : k_trace_ext<true, false>)
                           : (count ? k_trace_ext<false, true> : k_trace_ext<false, false>);
-    auto shade_k = sorted ? k_shade<true> : k_shade<false>;
+    const bool full = S.mext != nullptr;  // some material sets the full model's lobes
+    auto shade_k = full ? (sorted ? k_shade<true, false, true> : k_shade<false, false, true>)
+                        : (sorted ? k_shade<true> : k_shade<false>);
     auto shadow_k = count ? k_shadow<true> : k_shadow<false>;
     int g_trace = grid_for(ctx, trace_k, bt, tune.blocks_per_sm);
     int g_shade = grid_for(ctx, shade_k, bs, tune.blocks_per_sm);
@@ -920,10 +971,11 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     const DevScene& S = sc->ds;
     NrcNet& net = nrc->net;
     if (cfg.spp <= 0) throw Error(AQUA_ERR_INVALID_ARG, "spp must be positive");
-    if (cfg.max_depth < 0 || cfg.max_depth > 250) throw Error(AQUA_ERR_INVALID_ARG, "max_depth must be in [0, 250]");
+    check_depths(cfg.max_depth, cfg.rr_depth);
     if (cfg.nrc_train_samples < 0) throw Error(AQUA_ERR_INVALID_ARG, "nrc_train_samples must be >= 0");
     if (cfg.batch_size <= 0) throw Error(AQUA_ERR_INVALID_ARG, "batch_size must be positive");
-    size_t pixels = (size_t)S.cam.width * (size_t)S.cam.height;
+    WaveParams P{};
+    size_t pixels = plan_rows(cfg, S.cam, P);
     if (pixels == 0 || pixels > (1u << 27)) throw Error(AQUA_ERR_INVALID_ARG, "resolution out of range");
     const SlotPlan plan = plan_slots(pixels, cfg.spp, tune);
     const size_t slots = plan.slots;
@@ -950,7 +1002,6 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
         }
     }
     const bool visualize = cfg.visualize_cache != 0;
-    WaveParams P{};
     P.replicas = plan.replicas;
     P.seed = cfg.seed;
     P.spp = cfg.spp;
@@ -981,7 +1032,8 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     W.q_pix = nw.q_pix; W.q_raw = nw.q_raw; W.rec = nw.rec; W.ltrain = nw.ltrain; W.lsnap = nw.lsnap;
 
     auto trace_k = sorted ? k_trace_ext<true, false> : k_trace_ext<false, false>;
-    auto shade_k = sorted ? k_shade<true, true> : k_shade<false, true>;
+    auto shade_k = S.mext ? (sorted ? k_shade<true, true, true> : k_shade<false, true, true>)
+                          : (sorted ? k_shade<true, true> : k_shade<false, true>);
     auto shadow_k = k_shadow<false, true>;
     int g_trace = grid_for(ctx, trace_k, 128, tune.blocks_per_sm);
     int g_shade = grid_for(ctx, shade_k, 128, tune.blocks_per_sm);
@@ -1164,8 +1216,9 @@ void render_noalloc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cf
                     aqua_stats* stats) {
     const DevScene& S = sc->ds;
     if (cfg.spp <= 0) throw Error(AQUA_ERR_INVALID_ARG, "spp must be positive");
-    if (cfg.max_depth < 0) throw Error(AQUA_ERR_INVALID_ARG, "max_depth must be >= 0");
-    size_t pixels = (size_t)S.cam.width * (size_t)S.cam.height;
+    check_depths(cfg.max_depth, cfg.rr_depth);
+    WaveParams P{};
+    size_t pixels = plan_rows(cfg, S.cam, P);
     if (pixels == 0) throw Error(AQUA_ERR_INVALID_ARG, "resolution out of range");
     if (pixels > kNoAllocPixels)
         throw Error(AQUA_ERR_INVALID_ARG, "aqua_render_noalloc: " + std::to_string(pixels) +
@@ -1178,8 +1231,7 @@ void render_noalloc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cf
     char* base = (char*)noalloc_base(ctx->device);
     cudaStream_t st = ctx->stream;
 
-    WaveParams P{};  // zero: no replicas, no cache mode
-    P.seed = cfg.seed;
+    P.seed = cfg.seed;  // no replicas, no cache mode
     P.spp = cfg.spp;
     P.spp_offset = cfg.spp_offset;
     P.max_depth = cfg.max_depth;
@@ -1212,7 +1264,7 @@ void render_noalloc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cf
     AQ_CUDA(cudaMemsetAsync(W.stats, 0, 8 * kNoAllocStats, st));
 
     auto trace_k = k_trace_ext<false, false>;
-    auto shade_k = k_shade<false>;
+    auto shade_k = S.mext ? k_shade<false, false, true> : k_shade<false>;
     auto shadow_k = k_shadow<false>;
     int g_trace = grid_for(ctx, trace_k, 128, 0);
     int g_shade = grid_for(ctx, shade_k, 128, 0);

@@ -391,7 +391,7 @@ Bsdf_ read_bsdf(const Json& j, const std::string& dir, bool allow_missing, const
     const Json& p = j.obj[0].second;
     Bsdf_ b{};
     b.m.base_texture = -1;
-    b.m.reserved = 0;
+    b.m.reserved[0] = b.m.reserved[1] = 0;
     auto scalar = [&](const char* key, float dflt) {
         const Json* v = p.find(key);
         if (!v) return dflt;
@@ -420,6 +420,13 @@ Bsdf_ read_bsdf(const Json& j, const std::string& dir, bool allow_missing, const
     b.m.metallic = scalar("metallic", 0.0f);
     b.m.roughness = scalar("roughness", 0.5f);
     b.m.specular = scalar("specular", 0.5f);
+    b.m.specular_tint = scalar("specular_tint", 0.0f);
+    b.m.sheen = scalar("sheen", 0.0f);
+    b.m.sheen_tint = scalar("sheen_tint", 0.5f);
+    b.m.clearcoat = scalar("clearcoat", 0.0f);
+    b.m.clearcoat_roughness = scalar("clearcoat_roughness", 0.03f);
+    b.m.transmission = scalar("transmission", 0.0f);
+    b.m.ior = scalar("ior", 1.45f);
     const Json* em = p.find("emission");
     b.emission = mk(0, 0, 0);
     if (em) {
@@ -435,6 +442,13 @@ Bsdf_ read_bsdf(const Json& j, const std::string& dir, bool allow_missing, const
     unit("metallic", b.m.metallic);
     unit("roughness", b.m.roughness);
     unit("specular", b.m.specular);
+    unit("specular_tint", b.m.specular_tint);
+    unit("sheen", b.m.sheen);
+    unit("sheen_tint", b.m.sheen_tint);
+    unit("clearcoat", b.m.clearcoat);
+    unit("clearcoat_roughness", b.m.clearcoat_roughness);
+    unit("transmission", b.m.transmission);
+    if (!(b.m.ior >= 1.0f && b.m.ior <= 4.0f)) throw JsonError("bsdf \"" + name + "\": ior must lie in [1, 4]");
     if (!(base.x >= 0.0f && base.y >= 0.0f && base.z >= 0.0f))
         throw JsonError("bsdf \"" + name + "\": color must be non-negative");
     if (!(b.emission.x >= 0.0f && b.emission.y >= 0.0f && b.emission.z >= 0.0f))
@@ -541,7 +555,7 @@ HostScene load_scene_json(const std::string& path, bool allow_missing) {
             }
             MeshData md;
             try {
-                md = read_mesh_bson(dir + "/" + file);
+                md = read_mesh_bson(!file.empty() && file[0] == '/' ? file : dir + "/" + file);
             } catch (SceneError& e) {
                 if (e.status == AQUA_ERR_MISSING_ASSET && allow_missing) continue;
                 throw;
@@ -659,6 +673,7 @@ struct Builder {
         m.base_color[0] = color.x; m.base_color[1] = color.y; m.base_color[2] = color.z;
         m.base_texture = tex;
         m.metallic = metallic; m.roughness = roughness; m.specular = specular;
+        m.sheen_tint = 0.5f; m.clearcoat_roughness = 0.03f; m.ior = 1.45f;  // defaults of the unused lobes
         s.mats.push_back(m);
         s.mat_names.push_back("m" + std::to_string(s.mats.size() - 1));
         return (int)s.mats.size() - 1;

@@ -27,6 +27,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "aqua-engine_gb300"))
 
@@ -134,8 +136,12 @@ def sum_over_ranks(pg, x: float) -> float:
 
 
 def cpu_sample_run(threads: int, target_s: float, seed: int = 0):
-    """Oracle port (FP32, `threads` host threads) on a band of rows of the
-    workload at full spp; returns (Mpaths/s, description)."""
+    """Oracle port (FP32, `threads` host threads) on every k-th row of the
+    workload's image at full spp, k chosen for about target_s seconds, so the
+    sample covers the image uniformly (walls, boxes, light and floor in their
+    proportions); returns (Mpaths/s, seconds, description). The scene and its
+    BVH come from libaqua's host-only loader; only the rendering is timed,
+    and it is the oracle's."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import aqua
     import pyoracle
@@ -143,132 +149,151 @@ def cpu_sample_run(threads: int, target_s: float, seed: int = 0):
     hctx = aqua.Context(device=-2)
     scene = hctx.procedural(2, seed=0, width=WORKLOAD["width"], height=WORKLOAD["height"])
     orc = pyoracle.OracleScene.from_aqua(scene)
-    W = WORKLOAD["width"]
-    mid = (WORKLOAD["height"] // 2) * W
-    # calibrate on 2048 pixels (32 chunks of 64 for the thread pool), then
-    # size the band for ~target_s seconds
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    kw = dict(seed=seed, precision=32, rr_depth=WORKLOAD["rr_depth"], threads=threads)
+    # calibrate on 8 evenly spaced rows, then take every k-th row
+    cal = list(range(H // 16, H, H // 8))
     t0 = time.perf_counter()
-    orc.render(WORKLOAD["spp"], WORKLOAD["max_depth"], seed=seed, precision=32, rr_depth=WORKLOAD["rr_depth"],
-               threads=threads, pixel_begin=mid, pixel_end=mid + 2048)
-    dt = max(time.perf_counter() - t0, 1e-3)
-    npx = int(max(2048, min(W * 256, 2048 * target_s / dt)))
+    orc.render_rows(cal, WORKLOAD["spp"], WORKLOAD["max_depth"], **kw)
+    per_row = max(time.perf_counter() - t0, 1e-3) / len(cal)
+    step = max(1, int(np.ceil(H * per_row / target_s)))
+    rows = list(range(step // 2, H, step))
     t0 = time.perf_counter()
-    _, st = orc.render(WORKLOAD["spp"], WORKLOAD["max_depth"], seed=seed, precision=32,
-                       rr_depth=WORKLOAD["rr_depth"], threads=threads, pixel_begin=mid, pixel_end=mid + npx)
+    _, st = orc.render_rows(rows, WORKLOAD["spp"], WORKLOAD["max_depth"], **kw)
     dt = time.perf_counter() - t0
     paths = float(st[0])
     scene.free()
     hctx.close()
-    return paths / dt / 1e6, dt, f"{npx} pixels from the middle row of the 1024x1024 image, 1024 spp each " \
-                                  f"({int(paths)} paths, {dt:.1f} s)"
+    return paths / dt / 1e6, dt, f"one row in every {step} of the {W}x{H} image ({len(rows)} rows of {W} pixels, " \
+                                  f"{WORKLOAD['spp']} spp each: {int(paths)} paths, {dt:.1f} s); scene and BVH " \
+                                  f"built by libaqua's host-only loader, rendering by the oracle"
 
 
-NRC_WORKLOAD = {"workload": "interior-320x180-depth8-cache-vs-plain",
+NRC_WORKLOAD = {"workload": "interior-1920x1080-1spp-per-frame-cache-vs-plain",
                 "scene": "synthetic interior: 153 meshes, 1.15M triangles, 8 textures 2048^2, 16 quad lights, seed 0",
-                "width": 320, "height": 180, "max_depth": 8, "rr_depth": 3, "reference_spp": 65536,
-                "frame_spp": 32, "train_records_per_frame": 65536, "batch": 16384, "learning_rate": 1e-2,
-                "query_vertex": 4, "burn_in_frames": 8, "target_relmse": 1e-3, "ema_decay": 0.0,
-                "note": "the 1080p, 1-spp-per-frame cache workload scaled to 320x180: 32 spp per frame keeps "
-                        "1.8M paths and 65,536 training records per frame; queried at vertex 4 (allowed: vertex "
-                        ">= 2; vertex 2 / 3 / 5 measured 4.4x / 1.8x / 0.82x of the plain time)"}
-
+                "width": 1920, "height": 1080, "max_depth": 8, "rr_depth": 3, "frame_spp": 1,
+                "train_records_per_frame": 65536, "batch": 16384, "learning_rate": 1e-2, "query_vertex": 4,
+                "burn_in_frames": 16, "target_relmse": 1e-3, "ema_decay": 0.0, "plain_spp_per_call": 16,
+                "reference_spp": 65536, "reference_rows": "rows 8, 24, ..., 1064 (every 16th row, 67 rows)",
+                "error_rows": "the reference's rows: relMSE over every 16th row, an unbiased estimate of the "
+                              "whole image's relMSE",
+                "note": "cached renderer: 1 spp per 1920x1080 frame, online training on 65,536 records per frame "
+                        "(Adam, lr 1e-2), queried at vertex 4 (allowed: vertex >= 2), frames after the burn-in "
+                        "averaged; plain: the wavefront path tracer at 16 spp per call; both render whole frames "
+                        "and are timed by wall clock per call (error evaluation excluded)"}
+REF_ROW_BEGIN, REF_ROW_STEP = 8, 16
 
 _NRC_REF = {}
 
 
-def run_nrc_metric(ctx, budget_s: float = 60.0, overrides: dict | None = None):
-    """Time to relMSE 1e-3 against a 65,536-spp plain reference, for the plain
-    wavefront path tracer and for the cached renderer (online training
-    included in its time). Wall clock per render call; the error evaluation
-    between calls is excluded."""
+def nrc_reference(ctx, scene, W):
+    """65,536-spp plain reference of every 16th row (row subset render, the
+    same random-number streams as whole frames), cached per process."""
     import aqua
     import numpy as np
 
-    W = dict(NRC_WORKLOAD, **(overrides or {}))
-    scene = ctx.procedural(3, seed=0, width=W["width"], height=W["height"])
-    shape = (W["height"], W["width"], 3)
-
-    def rel_mse(x, r):
-        return float(np.mean((x.astype(np.float64) - r) ** 2 / (r * r + 1e-2)))
-
-    # Reference: 65,536 spp as 16 progressive calls (kept for later calls
-    # with the same image size in this process).
-    t0 = time.perf_counter()
     key = (W["width"], W["height"], W["reference_spp"], W["max_depth"])
     if key not in _NRC_REF:
-        acc = np.zeros(shape, np.float32)
+        rows = len(range(REF_ROW_BEGIN, W["height"], REF_ROW_STEP))
+        acc = np.zeros((rows, W["width"], 3), np.float32)
         chunk = W["reference_spp"] // 16
+        t0 = time.perf_counter()
         for k in range(16):
             ctx.render(scene, ctx.integrator(spp=chunk, max_depth=W["max_depth"], rr_depth=W["rr_depth"],
-                                             seed=424242, spp_offset=k * chunk), out=acc,
-                       flags=aqua.RENDER_ACCUMULATE)
-        _NRC_REF[key] = acc.astype(np.float64) / W["reference_spp"]
-    ref = _NRC_REF[key]
-    t_ref = time.perf_counter() - t0
+                                             seed=424242, spp_offset=k * chunk, row_begin=REF_ROW_BEGIN,
+                                             row_step=REF_ROW_STEP), out=acc, flags=aqua.RENDER_ACCUMULATE)
+        _NRC_REF[key] = (acc.astype(np.float64) / W["reference_spp"], time.perf_counter() - t0)
+    return _NRC_REF[key]
 
-    # Plain: 16 spp per call, running mean.
-    plain = {"spp": 0, "t": 0.0, "curve": []}
-    acc = np.zeros(shape, np.float32)
-    t_plain, e = None, 1.0
-    while plain["t"] < budget_s:
-        t0 = time.perf_counter()
-        ctx.render(scene, ctx.integrator(spp=16, max_depth=W["max_depth"], rr_depth=W["rr_depth"], seed=7,
-                                         spp_offset=plain["spp"]), out=acc, flags=aqua.RENDER_ACCUMULATE)
-        plain["t"] += time.perf_counter() - t0
-        plain["spp"] += 16
-        e = rel_mse(acc / plain["spp"], ref)
-        if plain["spp"] % 256 == 0:
-            plain["curve"].append((plain["spp"], round(plain["t"], 4), e))
-        if e <= W["target_relmse"]:
-            t_plain = plain["t"]
-            break
-    plain["relmse"] = e
 
-    # Cached: frames of 32 spp with online training; frames after the
-    # burn-in are averaged.
-    net = aqua.Nrc(ctx, seed=1, learning_rate=W["learning_rate"], ema_decay=W["ema_decay"])
-    cfg = lambda f: ctx.integrator(type=aqua.INTEGRATOR_NRC, spp=W["frame_spp"], max_depth=W["max_depth"],
-                                   rr_depth=W["rr_depth"], seed=1000 + f, nrc_query_vertex=W["query_vertex"],
-                                   nrc_train_samples=W["train_records_per_frame"], batch_size=W["batch"],
-                                   training_iters=0)
-    cached = {"frames": 0, "t": 0.0, "curve": [], "nrc_ms": 0.0}
-    acc = np.zeros(shape, np.float32)
-    frame_img = np.zeros(shape, np.float32)
-    t_cached, e, used = None, 1.0, 0
-    best = 1.0
-    while cached["t"] < budget_s:
-        t0 = time.perf_counter()
-        _, st = ctx.render_nrc(scene, cfg(cached["frames"]), net, out=frame_img)
-        cached["t"] += time.perf_counter() - t0
-        cached["nrc_ms"] += st.nrc_ms
-        cached["frames"] += 1
-        if cached["frames"] > W["burn_in_frames"]:
-            acc += frame_img
-            used += 1
-            e = rel_mse(acc / used, ref)
-            best = min(best, e)
-            if t_plain and "relmse_at_plain_time" not in cached and cached["t"] >= t_plain:
-                cached["relmse_at_plain_time"] = e
-            if used % 16 == 0:
-                cached["curve"].append((cached["frames"], round(cached["t"], 4), e))
+def run_nrc_metric(ctx, budget_s: float = 90.0, runs: int = 3, overrides: dict | None = None):
+    """Time to relMSE 1e-3 against a 65,536-spp plain reference, for the plain
+    wavefront path tracer and for the cached renderer at 1 spp per 1080p
+    frame (online training included in its time); `runs` runs per arm with
+    different seeds, medians reported. Wall clock per render call; the error
+    evaluation between calls (a device-to-host copy of the reference rows)
+    is excluded."""
+    import aqua
+    import numpy as np
+    import torch
+
+    W = dict(NRC_WORKLOAD, **(overrides or {}))
+    scene = ctx.procedural(3, seed=0, width=W["width"], height=W["height"])
+    ref, t_ref = nrc_reference(ctx, scene, W)
+    rows = torch.arange(REF_ROW_BEGIN, W["height"], REF_ROW_STEP, device="cuda")
+
+    def rel_mse(film_rows, n):
+        x = film_rows.double().cpu().numpy() / n
+        return float(np.mean((x - ref) ** 2 / (ref * ref + 1e-2)))
+
+    film = torch.zeros((W["height"], W["width"], 3), dtype=torch.float32, device="cuda")
+    plain_runs, cached_runs = [], []
+    for run in range(runs):
+        # Plain: plain_spp_per_call spp per call, running sum on the device.
+        film.zero_()
+        torch.cuda.synchronize()
+        spp, t, t_hit, e, curve = 0, 0.0, None, 1.0, []
+        k = W["plain_spp_per_call"]
+        while t < budget_s:
+            t0 = time.perf_counter()
+            ctx.render_device(scene, ctx.integrator(spp=k, max_depth=W["max_depth"], rr_depth=W["rr_depth"],
+                                                    seed=7 + run, spp_offset=spp), film.data_ptr(),
+                              flags=aqua.RENDER_ACCUMULATE)
+            t += time.perf_counter() - t0
+            spp += k
+            e = rel_mse(film[rows], spp)
+            if spp % 512 == 0:
+                curve.append((spp, round(t, 3), e))
             if e <= W["target_relmse"]:
-                t_cached = cached["t"]
+                t_hit = t
                 break
-    cached["relmse"] = e
-    cached["best_relmse"] = best
-    net.free()
+        plain_runs.append({"time_s": t_hit, "spp": spp, "relmse": e, "curve": curve[-4:]})
+
+        # Cached: 1 spp per frame with online training; frames after the
+        # burn-in are summed on the device.
+        net = aqua.Nrc(ctx, seed=1 + run, learning_rate=W["learning_rate"], ema_decay=W["ema_decay"])
+        scratch = torch.zeros_like(film)
+        film.zero_()
+        torch.cuda.synchronize()
+        frames, used, t, t_hit, e, curve, nrc_ms = 0, 0, 0.0, None, 1.0, [], 0.0
+        while t < budget_s:
+            burn = frames < W["burn_in_frames"]
+            cfg = ctx.integrator(type=aqua.INTEGRATOR_NRC, spp=W["frame_spp"], max_depth=W["max_depth"],
+                                 rr_depth=W["rr_depth"], seed=1000 * (run + 1) + frames,
+                                 nrc_query_vertex=W["query_vertex"], nrc_train_samples=W["train_records_per_frame"],
+                                 batch_size=W["batch"], training_iters=0)
+            t0 = time.perf_counter()
+            _, st = ctx.render_nrc(scene, cfg, net, dev_ptr=(scratch if burn else film).data_ptr(),
+                                   flags=0 if burn else aqua.RENDER_ACCUMULATE)
+            t += time.perf_counter() - t0
+            nrc_ms += st.nrc_ms
+            frames += 1
+            if burn:
+                continue
+            used += 1
+            if used % 16 == 0:
+                e = rel_mse(film[rows], used * W["frame_spp"])
+                if used % 256 == 0:
+                    curve.append((frames, round(t, 3), e))
+                if e <= W["target_relmse"]:
+                    t_hit = t
+                    break
+        net.free()
+        cached_runs.append({"time_s": t_hit, "frames": frames, "relmse": e, "mlp_ms_total": round(nrc_ms, 1),
+                            "ms_per_frame": 1e3 * t / max(frames, 1), "curve": curve[-4:]})
     scene.free()
-    # The reference's own error, extrapolated from the plain curve (1/N).
-    ref_err = plain["relmse"] * plain["spp"] / W["reference_spp"]
-    out = {"config": W, "reference_s": round(t_ref, 2), "reference_relmse_est": ref_err,
-           "plain": {"time_s": t_plain, "spp": plain["spp"], "relmse": plain["relmse"], "curve": plain["curve"][-6:]},
-           "cached": {"time_s": t_cached, "frames": cached["frames"], "relmse": cached["relmse"],
-                      "best_relmse": best, "mlp_ms_total": round(cached["nrc_ms"], 2),
-                      "relmse_at_plain_time": cached.get("relmse_at_plain_time"),
-                      "curve": cached["curve"][-6:]},
-           "time_ratio_cached_over_plain": (t_cached / t_plain) if (t_cached and t_plain) else None,
-           "budget_s": budget_s}
-    return out
+
+    def med(xs):
+        xs = [x for x in xs if x is not None]
+        return statistics.median(xs) if len(xs) == len(plain_runs) else None
+
+    tp = med([r["time_s"] for r in plain_runs])
+    tc = med([r["time_s"] for r in cached_runs])
+    return {"config": W, "runs": runs, "reference_s": round(t_ref, 2),
+            "plain": {"time_s_median": tp, "runs": plain_runs},
+            "cached": {"time_s_median": tc, "runs": cached_runs},
+            "time_ratio_cached_over_plain": (tc / tp) if (tc and tp) else None,
+            "budget_s_per_run": budget_s}
 
 
 def measure_l2_copy_gbs(device: int) -> dict:
@@ -301,16 +326,56 @@ def measure_l2_copy_gbs(device: int) -> dict:
 INTERIOR_WORKLOAD = {"workload": "interior-1920x1080-256spp-depth8", "width": 1920, "height": 1080, "spp": 256,
                      "max_depth": 8, "scene": "synthetic interior: 153 meshes, 1.15M triangles, 8 textures, "
                                               "16 quad lights, seed 0"}
+SPHERES_WORKLOAD = {"workload": "sphere-field-1024x1024-64spp-depth8", "width": 1024, "height": 1024, "spp": 64,
+                    "max_depth": 8, "scene": "random-sphere field: 4.0M triangles, seed 0"}
+# DRAM bytes (read + write) of one full-queue k_trace_ext launch from ncu
+# captures of these scenes, and the rays that launch traced.
+TRACE_TRAFFIC = {
+    "interior": {"bytes": 564.4e6, "rays": 2073600,
+                 "source": "profiles/trace_interior-1920x1080-256spp.md (497.3 MB read + 67.1 MB written)"},
+}
 
 
-def run_interior_metric(ctx, warmup: int = 1, steps: int = 2):
-    """Plain path tracing of the interior at 1080p, 256 spp (one step = the
-    whole image)."""
-    import torch
+def trace_roofline(ctx, scene, cfg, film_ptr, hbm_peak, peak_src, l2_gbs, count_spp, traffic=None):
+    """Roofline of k_trace_ext on one scene: algorithmic bytes per ray from a
+    counting pass at count_spp (node visits x NODE_BYTES + triangle tests x
+    48 + 48 B of ray and hit), times the rays per launch of a full render,
+    over the mean launch time from CUDA events around every 8th launch of
+    that render (RENDER_STAGE_TIMING; an extra render outside the timed
+    steps)."""
     import aqua
 
-    W = INTERIOR_WORKLOAD
-    scene = ctx.procedural(3, seed=0, width=W["width"], height=W["height"])
+    ccfg = ctx.integrator(spp=count_spp, max_depth=cfg.max_depth, rr_depth=cfg.rr_depth, seed=cfg.seed)
+    cst = ctx.render_device(scene, ccfg, film_ptr, flags=aqua.RENDER_COUNT)
+    bytes_per_ray = (cst.node_visits * NODE_BYTES + cst.tri_tests * 48) / max(cst.ext_rays, 1) + 48
+    st = ctx.render_device(scene, cfg, film_ptr, flags=aqua.RENDER_STAGE_TIMING)
+    rays_per_launch = st.ext_rays / max(st.iterations, 1)
+    avg_launch_s = st.trace_ms * 1e-3 / max(st.trace_launches, 1)
+    achieved = bytes_per_ray * rays_per_launch / avg_launch_s / 1e9
+    out = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+           "peak_source": peak_src, "kernel": "k_trace_ext (closest-hit BVH traversal)",
+           "bytes_per_ray": bytes_per_ray, "rays_per_launch": rays_per_launch,
+           "avg_launch_us": avg_launch_s * 1e6, "frac_of_l2_copy": achieved / l2_gbs if l2_gbs else None,
+           "node_visits_per_ray": cst.node_visits / max(cst.ext_rays, 1),
+           "tri_tests_per_ray": cst.tri_tests / max(cst.ext_rays, 1), "counting_spp": count_spp,
+           "traffic": None}
+    if traffic:
+        per_ray = traffic["bytes"] / traffic["rays"]
+        out["traffic"] = per_ray * rays_per_launch
+        out["traffic_note"] = (f"ncu DRAM bytes of a full-queue launch ({traffic['rays']} rays) scaled to this "
+                               f"launch's mean ray count; {traffic['source']}")
+        out["dram_gbs"] = out["traffic"] / avg_launch_s / 1e9
+        out["dram_frac"] = out["dram_gbs"] / hbm_peak
+    return out
+
+
+def run_scene_metric(ctx, config_id: int, W: dict, hbm_peak: float, peak_src: str, l2_gbs: float,
+                     warmup: int = 1, steps: int = 2, traffic=None):
+    """Plain path tracing of one procedural scene (one step = the whole
+    image), with the traversal roofline of that workload."""
+    import torch
+
+    scene = ctx.procedural(config_id, seed=0, width=W["width"], height=W["height"])
     film = torch.zeros(W["width"] * W["height"] * 3, dtype=torch.float32, device="cuda")
     cfg = ctx.integrator(spp=W["spp"], max_depth=W["max_depth"], rr_depth=3, seed=1)
     torch.cuda.synchronize()
@@ -318,15 +383,20 @@ def run_interior_metric(ctx, warmup: int = 1, steps: int = 2):
         ctx.render_device(scene, cfg, film.data_ptr())
     ms, paths, rays = 0.0, 0, 0
     for _ in range(steps):
-        torch.cuda.nvtx.range_push("interior_step")
+        torch.cuda.nvtx.range_push(f"scene{config_id}_step")
         st = ctx.render_device(scene, cfg, film.data_ptr())
         torch.cuda.nvtx.range_pop()
         ms += st.device_ms
         paths += st.paths
         rays += st.ext_rays + st.shadow_rays
+    roof = trace_roofline(ctx, scene, cfg, film.data_ptr(), hbm_peak, peak_src, l2_gbs, count_spp=16,
+                          traffic=traffic)
+    info = scene.info()
     scene.free()
-    return {"config": W, "value": paths / (ms * 1e-3) / 1e6, "unit": "Mpaths/s", "mrays_per_s": rays / (ms * 1e-3) / 1e6,
-            "ms_per_step": ms / steps, "steps": steps, "warmup": warmup}
+    return {"config": dict(W, triangles=info.num_triangles, bvh_nodes=info.num_bvh_nodes,
+                           scene_device_mb=round(info.device_bytes / 1e6, 1)),
+            "value": paths / (ms * 1e-3) / 1e6, "unit": "Mpaths/s", "mrays_per_s": rays / (ms * 1e-3) / 1e6,
+            "ms_per_step": ms / steps, "steps": steps, "warmup": warmup, "roofline": roof}
 
 
 NRC_INFER_WORKLOAD = {"workload": "nrc-inference-16777216-rows", "rows": 1 << 24,
@@ -449,7 +519,8 @@ def run_reference(args, world, rank, pg):
                              "sample": desc},
             "e2e": {"value": value, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "reference crate has no implementation (src/lib.rs is empty); this arm times the CPU "
-                    "oracle port of the same estimator"}
+                    "oracle port of the same estimator; the scene and BVH are built by libaqua's host-only loader "
+                    "(untimed) and only the rendering, the oracle's, is timed"}
     print(json.dumps(line), flush=True)
 
 
@@ -493,7 +564,7 @@ def run_gpu(args, world, rank, local, pg):
             flush.zero_()
             torch.cuda.synchronize()
             torch.cuda.nvtx.range_push("timed_step")
-            steps.append(ctx.render_device(scene, cfg, film.data_ptr(), tune, flags=aqua.RENDER_STAGE_TIMING))
+            steps.append(ctx.render_device(scene, cfg, film.data_ptr(), tune))
             torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
@@ -505,9 +576,15 @@ def run_gpu(args, world, rank, local, pg):
     all_paths = sum_over_ranks(pg, paths)
     value = all_paths / (ms_max * 1e-3) / 1e6
 
-    # Dominant kernel: closest-hit traversal.
-    trace_ms = sum(s.trace_ms for s in steps)
-    launches = sum(s.trace_launches for s in steps)
+    # Dominant kernel: closest-hit traversal. Its launch times come from one
+    # more render of the same step with CUDA events around every 8th
+    # iteration's launches (RENDER_STAGE_TIMING), run after the timed steps
+    # so the events do not stretch them.
+    flush.zero_()
+    torch.cuda.synchronize()
+    staged = ctx.render_device(scene, cfg, film.data_ptr(), tune, flags=aqua.RENDER_STAGE_TIMING)
+    trace_ms = staged.trace_ms
+    launches = staged.trace_launches
     ext = cst.ext_rays
     bytes_step = cst.node_visits * NODE_BYTES + cst.tri_tests * 48 + ext * (32 + 16)
     bytes_per_launch = bytes_step / max(cst.trace_launches, 1)
@@ -521,27 +598,36 @@ def run_gpu(args, world, rank, local, pg):
                         "child links) + triangle tests x 48 B + 48 B per ray; the Cornell BVH (8 nodes) is "
                         "cache-resident, so DRAM traffic is far below this"}
 
-    # End to end through the C ABI with host buffers: scene upload + render
-    # + film download every step.
+    # End to end through the C ABI with host buffers: scene upload from
+    # pinned host memory + render + film download every step, over the same
+    # step count as `value` and with the same L2 flush before each step
+    # (outside the timed stretch).
     host_film = None
-    e2e_steps = max(1, min(args.steps, 3))
     barrier(pg)
-    t0 = time.perf_counter()
-    e2e_paths = 0
-    for _ in range(e2e_steps):
+    e2e_s, e2e_paths = 0.0, 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         scene.upload()
         host_film, st = ctx.render(scene, cfg, tune, out=host_film)
+        e2e_s += time.perf_counter() - t0
         e2e_paths += st.paths
-    e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
+    e2e_s = max_over_ranks(pg, e2e_s)
     e2e_value = sum_over_ranks(pg, e2e_paths) / e2e_s / 1e6
 
     l2 = measure_l2_copy_gbs(local)
     roofline["l2_copy_gbs"] = l2["gbs"]
     roofline["frac_of_l2_copy"] = achieved / l2["gbs"]
-    interior = run_interior_metric(ctx) if rank == 0 and not args.no_interior else None
+    interior = spheres = None
+    if rank == 0 and not args.no_interior:
+        interior = run_scene_metric(ctx, 3, INTERIOR_WORKLOAD, hbm_peak, peak_src, l2["gbs"],
+                                    traffic=TRACE_TRAFFIC.get("interior"))
+        spheres = run_scene_metric(ctx, 5, SPHERES_WORKLOAD, hbm_peak, peak_src, l2["gbs"],
+                                   traffic=TRACE_TRAFFIC.get("spheres"))
     nrc = None
     if rank == 0 and not args.no_nrc and not args.no_nrc_time:
-        nrc = run_nrc_metric(ctx, args.nrc_budget)
+        nrc = run_nrc_metric(ctx, args.nrc_budget, args.nrc_runs)
     batch = None
     if rank == 0 and not args.no_batch:
         batch = run_batch_metric(ctx, spp_div=args.batch_spp_div)
@@ -571,16 +657,20 @@ def run_gpu(args, world, rank, local, pg):
                 "mrays_per_s": sum_over_ranks(pg, sum(s.ext_rays + s.shadow_rays for s in steps)) /
                                (ms_max * 1e-3) / 1e6,
                 "wall_s": wall, "clocks": clk.summary(), "roofline": roofline, "cpu_baseline": cpu,
-                "e2e": {"value": e2e_value, "unit": "Mpaths/s", "h2d_bytes_per_step": int(info.upload_bytes),
+                "e2e": {"value": e2e_value, "unit": "Mpaths/s", "steps": args.steps,
+                        "timing": "wall clock per step around scene upload + aqua_render + film download, "
+                                  "L2 flushed before each step outside the timed stretch",
+                        "h2d_bytes_per_step": int(info.upload_bytes),
                         "d2h_bytes_per_step": int(info.width * info.height * 12)},
                 "gpu_launches": gpu_launches,
                 "interior": interior,
+                "sphere_field": spheres,
                 "nrc_time_to_relmse": nrc,
                 "nrc_inference": nrc_inf,
                 "batch": batch,
-                "stage_ms_per_step": {"trace": trace_ms / args.steps,
-                                      "shade": sum(s.shade_ms for s in steps) / args.steps,
-                                      "shadow": sum(s.shadow_ms for s in steps) / args.steps}}
+                "stage_ms_sampled": {"trace": staged.trace_ms, "shade": staged.shade_ms, "shadow": staged.shadow_ms,
+                                     "note": "device ms of every 8th iteration's launches of one render of the "
+                                             "step (RENDER_STAGE_TIMING), i.e. about 1/8 of each stage's time"}}
         print(json.dumps(line), flush=True)
     scene.free()
     ctx.close()
@@ -598,7 +688,8 @@ def main():
     ap.add_argument("--no-nrc-time", action="store_true", help="skip the cached-vs-plain time-to-relMSE measurement")
     ap.add_argument("--nrc-rows", type=int, default=NRC_INFER_WORKLOAD["rows"],
                     help="rows of the cache-inference measurement (smaller only for profiling captures)")
-    ap.add_argument("--nrc-budget", type=float, default=60.0, help="seconds per arm of that measurement")
+    ap.add_argument("--nrc-budget", type=float, default=90.0, help="seconds per run and arm of that measurement")
+    ap.add_argument("--nrc-runs", type=int, default=3, help="runs per arm of that measurement (median reported)")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-job batched-serving measurement")
     ap.add_argument("--batch-spp-div", type=int, default=1,
                     help="divide every batch job's spp by this (profiling captures only)")

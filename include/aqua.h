@@ -95,8 +95,10 @@ enum { AQUA_INTEGRATOR_PATH = 0, AQUA_INTEGRATOR_NRC = 1 };
 typedef struct aqua_integrator_cfg {
     int32_t type;            /* AQUA_INTEGRATOR_PATH or AQUA_INTEGRATOR_NRC */
     int32_t spp;             /* samples per pixel                           */
-    int32_t max_depth;       /* bounces; NEE at vertices 0..max_depth-1     */
-    int32_t rr_depth;        /* Russian roulette from this bounce on        */
+    int32_t max_depth;       /* bounces; NEE at vertices 0..max_depth-1;
+                                [0, 250], else AQUA_ERR_INVALID_ARG          */
+    int32_t rr_depth;        /* Russian roulette from this bounce on; [0, 250]
+                                (above max_depth: no roulette)              */
     int32_t batch_size;      /* NRC: training batch (integrator.json:4)     */
     int32_t training_iters;  /* NRC: optimizer steps per frame              */
     float learning_rate;     /* NRC: Adam step size (integrator.json:7)     */
@@ -105,6 +107,14 @@ typedef struct aqua_integrator_cfg {
     int32_t spp_offset;      /* first sample index (progressive rendering)  */
     int32_t nrc_train_samples; /* NRC: training records per frame          */
     int32_t nrc_query_vertex;  /* NRC: query the cache at this vertex (>= 2; default 4) */
+    /* Row subset (wavefront renders): with row_step > 1 only the camera
+     * image's rows row_begin, row_begin + row_step, ... are rendered, and
+     * rgb_out holds just those rows in order (rows x width x 3). Every pixel
+     * keeps the random-number stream of its place in the full image, so the
+     * rows equal the same rows of a full render with the same seed. 0 or 1 =
+     * the whole image (row_begin 0). The persistent kernel renders whole
+     * images only (aqua_render then runs the wavefront). */
+    int32_t row_begin, row_step;
     int32_t reserved0;
 } aqua_integrator_cfg;
 
@@ -191,11 +201,21 @@ typedef struct aqua_camera {
 } aqua_camera;
 
 /* Material, the Lambert + GGX subset of `Principled` (scenes/cbox.json:3-62). */
+/* The `Principled` parameters (scenes/cbox.json:3-62) the renderer
+ * consumes. Lambert diffuse, sheen (Burley 2012), GGX specular with
+ * Schlick Fresnel and specular tint, a clearcoat GTR1 lobe (Burley 2012)
+ * and a rough dielectric transmission lobe (Walter et al. 2007) with the
+ * given ior. subsurface*, anisotropic* and `hint` are not consumed. All
+ * weights lie in [0, 1]; ior in [1, 4]. */
 typedef struct aqua_material {
     float base_color[3];      /* linear RGB (Srgb values are decoded)       */
     int32_t base_texture;     /* -1 = none, else texture index              */
     float metallic, roughness, specular;
-    int32_t reserved;
+    float specular_tint;      /* dielectric F0 tinted toward the base hue   */
+    float sheen, sheen_tint;
+    float clearcoat, clearcoat_roughness;
+    float transmission, ior;  /* glass lobe weight (1-metallic)*transmission */
+    int32_t reserved[2];
 } aqua_material;
 
 enum { AQUA_LIGHT_QUAD = 0, AQUA_LIGHT_POINT = 1, AQUA_LIGHT_TRIANGLE = 2 };
@@ -236,7 +256,7 @@ AQUA_API const char* aqua_status_string(aqua_status s);
 /* ABI version: 100 x major + minor. Major 2: aqua_scene_export_bvh returns
  * the four-wide tree (32 floats per node; major 1 returned a binary tree of
  * 16 floats per node). */
-#define AQUA_VERSION 200
+#define AQUA_VERSION 300
 AQUA_API int aqua_version(void);
 
 /* ---------------------------------------------------------------- scenes */
@@ -456,7 +476,9 @@ AQUA_API aqua_status aqua_render_nrc(aqua_ctx* ctx, aqua_scene* scene, const aqu
  *
  * The first call on a device looks up the array's device address (a
  * one-time set-up per device); make that first call before any stream
- * capture. Every call shares the array and clears what it needs; calls
+ * capture. The address is kept for the life of the process: a device reset
+ * (cudaDeviceReset) unloads the array, and the library must not be used on
+ * that device afterwards. Every call shares the array and clears what it needs; calls
  * whose work overlaps on the GPU (other contexts or threads at the same
  * time) race on it and must be serialised by the caller. stats may be NULL;
  * its timing fields stay 0. */

@@ -306,27 +306,52 @@ void parallel_for(int64_t n, int threads, F&& f) {
 }
 
 // ------------------------------------------------------------------ BSDF
-// Lambert + GGX, same definitions as the device (see oracle.h).
+// The `Principled` model (scenes/cbox.json:3-62), restated from its
+// published lobes (see oracle.h): Lambert diffuse and sheen (Burley 2012),
+// GGX / Trowbridge-Reitz specular with height-correlated Smith masking and
+// Schlick Fresnel (Walter et al. 2007), visible-normal sampling (Heitz 2018),
+// a rough dielectric reflection/refraction lobe with exact Fresnel (Walter
+// et al. 2007) and a GTR1 clearcoat (Burley 2012). With specular_tint,
+// sheen, clearcoat and transmission all 0 the terms reduce to Lambert + GGX.
 template <class T>
 struct Mat {
-    V3<T> color, F0;
+    V3<T> color, F0, sheen;
     T metallic, alpha, p_spec;
     bool has_spec;
+    T wdiff, wspec, wglass, eta, cc, cc_a2, p_glass, p_cc;
 };
+template <class T> T lum3(V3<T> c) { return T(0.2126) * c.x + T(0.7152) * c.y + T(0.0722) * c.z; }
+template <class T> V3<T> mix3(V3<T> a, V3<T> b, T t) { return a + (b - a) * t; }
 template <class T>
-Mat<T> make_mat(V3<T> color, T metallic, T roughness, T specular) {
+Mat<T> make_mat(V3<T> color, T metallic, T roughness, T specular, T spec_tint, T sheen, T sheen_tint, T clearcoat,
+                T cc_rough, T tr, T ior, bool front) {
     Mat<T> m;
     m.color = color;
     m.metallic = metallic;
     m.alpha = std::max(roughness * roughness, T(1e-3));
-    T f0d = T(0.08) * specular;
-    m.F0 = {f0d + (color.x - f0d) * metallic, f0d + (color.y - f0d) * metallic, f0d + (color.z - f0d) * metallic};
-    m.has_spec = (m.F0.x + m.F0.y + m.F0.z) > T(0);
-    T ws = luminance(m.F0), wd = (T(1) - metallic) * luminance(color);
+    const T lc = lum3(color);
+    const V3<T> one{1, 1, 1};
+    const V3<T> tint = lc > T(0) ? color * (T(1) / lc) : one;
+    V3<T> f0d = mix3(one, tint, spec_tint) * (T(0.08) * specular);
+    m.F0 = mix3(f0d, color, metallic);
+    m.wdiff = (T(1) - metallic) * (T(1) - tr);
+    m.wglass = (T(1) - metallic) * tr;
+    m.wspec = T(1) - m.wglass;
+    m.has_spec = (m.F0.x + m.F0.y + m.F0.z) > T(0) && m.wspec > T(0);
+    m.sheen = mix3(one, tint, sheen_tint) * (m.wdiff * sheen);
+    T e = std::max(ior, T(1.001));
+    m.eta = front ? e : T(1) / e;
+    m.cc = T(0.25) * clearcoat;
+    T ca = std::min(std::max(cc_rough * cc_rough, T(1e-3)), T(0.999));
+    m.cc_a2 = ca * ca;
+    T ws = m.has_spec ? lum3(m.F0) * m.wspec : T(0);
+    T wd = m.wdiff * lc + lum3(m.sheen);
     T ps = (ws + wd) > T(0) ? ws / (ws + wd) : T(0.5);
     if (ws > T(0) && wd > T(0)) ps = std::min(std::max(ps, T(0.1)), T(0.9));
-    if (!m.has_spec) ps = T(0);
-    m.p_spec = ps;
+    m.p_spec = m.has_spec ? ps : T(0);
+    T tot = wd + ws + m.wglass + m.cc;
+    m.p_glass = m.wglass > T(0) ? m.wglass / tot : T(0);
+    m.p_cc = m.cc > T(0) ? m.cc / tot : T(0);
     return m;
 }
 template <class T> T D_ggx(T a2, T c) {
@@ -337,55 +362,143 @@ template <class T> T Lambda(T a2, T c) {
     T t2 = std::max(T(1) - c * c, T(0)) / (c * c);
     return T(0.5) * (-T(1) + std::sqrt(T(1) + a2 * t2));
 }
+template <class T> T D_gtr1(T a2, T c) { return (a2 - T(1)) / (T(M_PI) * std::log(a2) * (T(1) + (a2 - T(1)) * c * c)); }
+template <class T> T pow5(T x) { return (x * x) * (x * x) * x; }
+// Unpolarised Fresnel reflectance of a dielectric interface: cos_i >= 0 on
+// the incident side, eta = n(transmitted) / n(incident).
+template <class T> T fresnel_diel(T ci, T eta) {
+    T s2 = (T(1) - ci * ci) / (eta * eta);
+    if (s2 >= T(1)) return T(1);
+    T ct = std::sqrt(T(1) - s2);
+    T rs = (ci - eta * ct) / (ci + eta * ct), rp = (eta * ci - ct) / (eta * ci + ct);
+    return T(0.5) * (rs * rs + rp * rp);
+}
+template <class T> V3<T> refr_half(V3<T> wo, V3<T> wi, T eta) {
+    V3<T> h = unit(wo + wi * eta);
+    return h.z < T(0) ? -h : h;
+}
 template <class T> V3<T> eval(const Mat<T>& m, V3<T> wo, V3<T> wi) {
-    if (wo.z <= T(0) || wi.z <= T(0)) return {0, 0, 0};
-    V3<T> f = m.color * ((T(1) - m.metallic) / T(M_PI));
-    if (!m.has_spec) return f;
+    if (wo.z <= T(0) || wi.z == T(0)) return {0, 0, 0};
+    const T a2 = m.alpha * m.alpha;
+    if (wi.z < T(0)) {
+        if (!(m.wglass > T(0))) return {0, 0, 0};
+        V3<T> h = refr_half(wo, wi, m.eta);
+        T co = dot3(wo, h), ci = dot3(wi, h);
+        if (!(co > T(0) && ci < T(0))) return {0, 0, 0};
+        T F = fresnel_diel(co, m.eta), den = co + m.eta * ci;
+        T G2 = T(1) / (T(1) + Lambda(a2, wo.z) + Lambda(a2, wi.z));
+        return m.color * (m.wglass * (T(1) - F) * D_ggx(a2, h.z) * G2 * (-ci) * co / (-wi.z * wo.z * den * den));
+    }
+    V3<T> f = m.color * (m.wdiff / T(M_PI));
     V3<T> h = wo + wi;
     T hl = len3(h);
-    if (hl > T(0)) {
-        h = h * (T(1) / hl);
-        T a2 = m.alpha * m.alpha;
+    if (!(hl > T(0))) return f;
+    h = h * (T(1) / hl);
+    const T wih = dot3(wi, h);
+    const T c = std::min(std::max(T(1) - wih, T(0)), T(1));
+    f = f + m.sheen * pow5(c);
+    const T den = T(4) * wo.z * wi.z;
+    if (m.has_spec || m.wglass > T(0)) {
         T D = D_ggx(a2, h.z);
         T G2 = T(1) / (T(1) + Lambda(a2, wo.z) + Lambda(a2, wi.z));
-        T c = std::min(std::max(T(1) - dot3(wi, h), T(0)), T(1));
-        T c5 = c * c * c * c * c;
-        V3<T> F{m.F0.x + (T(1) - m.F0.x) * c5, m.F0.y + (T(1) - m.F0.y) * c5, m.F0.z + (T(1) - m.F0.z) * c5};
-        f = f + F * (D * G2 / (T(4) * wo.z * wi.z));
+        if (m.has_spec) {
+            T c5 = pow5(c);
+            V3<T> F{m.F0.x + (T(1) - m.F0.x) * c5, m.F0.y + (T(1) - m.F0.y) * c5, m.F0.z + (T(1) - m.F0.z) * c5};
+            f = f + F * (D * G2 / den * m.wspec);
+        }
+        if (m.wglass > T(0)) {
+            T v = m.wglass * fresnel_diel(dot3(wo, h), m.eta) * D * G2 / den;
+            f = f + V3<T>{v, v, v};
+        }
+    }
+    if (m.cc > T(0)) {
+        const T ga2 = T(0.0625);
+        T G = T(1) / ((T(1) + Lambda(ga2, wo.z)) * (T(1) + Lambda(ga2, wi.z)));
+        T v = m.cc * D_gtr1(m.cc_a2, h.z) * (T(0.04) + T(0.96) * pow5(c)) * G / den;
+        f = f + V3<T>{v, v, v};
     }
     return f;
 }
 template <class T> T pdf(const Mat<T>& m, V3<T> wo, V3<T> wi) {
-    if (wo.z <= T(0) || wi.z <= T(0)) return T(0);
-    T pd = wi.z / T(M_PI), ps = T(0);
-    if (m.p_spec > T(0)) {
-        V3<T> h = wo + wi;
-        T hl = len3(h);
-        if (hl > T(0)) {
-            h = h * (T(1) / hl);
-            T a2 = m.alpha * m.alpha;
-            ps = D_ggx(a2, h.z) / ((T(1) + Lambda(a2, wo.z)) * T(4) * wo.z);
-        }
+    if (wo.z <= T(0) || wi.z == T(0)) return T(0);
+    const T a2 = m.alpha * m.alpha;
+    const T G1 = T(1) / (T(1) + Lambda(a2, wo.z));
+    if (wi.z < T(0)) {
+        if (!(m.p_glass > T(0))) return T(0);
+        V3<T> h = refr_half(wo, wi, m.eta);
+        T co = dot3(wo, h), ci = dot3(wi, h);
+        if (!(co > T(0) && ci < T(0))) return T(0);
+        T F = fresnel_diel(co, m.eta), den = co + m.eta * ci;
+        return m.p_glass * (T(1) - F) * G1 * D_ggx(a2, h.z) * co / wo.z * (m.eta * m.eta * (-ci) / (den * den));
     }
-    return (T(1) - m.p_spec) * pd + m.p_spec * ps;
+    T pd = wi.z / T(M_PI), ps = T(0), pg = T(0), pc = T(0);
+    V3<T> h = wo + wi;
+    T hl = len3(h);
+    if (hl > T(0)) {
+        h = h * (T(1) / hl);
+        T pv = G1 * D_ggx(a2, h.z) / (T(4) * wo.z);
+        if (m.p_spec > T(0)) ps = pv;
+        if (m.p_glass > T(0)) pg = fresnel_diel(dot3(wo, h), m.eta) * pv;
+        if (m.p_cc > T(0)) pc = D_gtr1(m.cc_a2, h.z) * h.z / (T(4) * dot3(wo, h));
+    }
+    T base = (T(1) - m.p_spec) * pd + m.p_spec * ps;
+    return (T(1) - m.p_glass - m.p_cc) * base + m.p_glass * pg + m.p_cc * pc;
 }
-template <class T> V3<T> sample(const Mat<T>& m, V3<T> wo, T ul, T u1, T u2) {
-    if (ul < m.p_spec) {
-        T a = m.alpha;
-        V3<T> Vh = unit(V3<T>{a * wo.x, a * wo.y, wo.z});
-        T l2 = Vh.x * Vh.x + Vh.y * Vh.y;
-        V3<T> T1 = l2 > T(0) ? V3<T>{-Vh.y, Vh.x, T(0)} * (T(1) / std::sqrt(l2)) : V3<T>{1, 0, 0};
-        V3<T> T2 = cross3(Vh, T1);
-        T r = std::sqrt(u1), phi = T(2 * M_PI) * u2;
-        T t1 = r * std::cos(phi), t2 = r * std::sin(phi);
-        T s = T(0.5) * (T(1) + Vh.z);
-        t2 = (T(1) - s) * std::sqrt(std::max(T(1) - t1 * t1, T(0))) + s * t2;
-        V3<T> Nh = T1 * t1 + T2 * t2 + Vh * std::sqrt(std::max(T(0), T(1) - t1 * t1 - t2 * t2));
-        V3<T> Ne = unit(V3<T>{a * Nh.x, a * Nh.y, std::max(T(0), Nh.z)});
-        return Ne * (T(2) * dot3(wo, Ne)) - wo;
-    }
+template <class T> V3<T> vndf(T a, V3<T> wo, T u1, T u2) {
+    V3<T> Vh = unit(V3<T>{a * wo.x, a * wo.y, wo.z});
+    T l2 = Vh.x * Vh.x + Vh.y * Vh.y;
+    V3<T> T1 = l2 > T(0) ? V3<T>{-Vh.y, Vh.x, T(0)} * (T(1) / std::sqrt(l2)) : V3<T>{1, 0, 0};
+    V3<T> T2 = cross3(Vh, T1);
     T r = std::sqrt(u1), phi = T(2 * M_PI) * u2;
-    return {r * std::cos(phi), r * std::sin(phi), std::sqrt(std::max(T(0), T(1) - u1))};
+    T t1 = r * std::cos(phi), t2 = r * std::sin(phi);
+    T s = T(0.5) * (T(1) + Vh.z);
+    t2 = (T(1) - s) * std::sqrt(std::max(T(1) - t1 * t1, T(0))) + s * t2;
+    V3<T> Nh = T1 * t1 + T2 * t2 + Vh * std::sqrt(std::max(T(0), T(1) - t1 * t1 - t2 * t2));
+    return unit(V3<T>{a * Nh.x, a * Nh.y, std::max(T(0), Nh.z)});
+}
+// wi.z > 0 reflection, < 0 refraction (glass lobe), 0 no sample: a
+// reflection below the surface or a refraction above it is no sample, so
+// every returned direction has the density pdf() reports.
+template <class T> V3<T> sample(const Mat<T>& m, V3<T> wo, T ul, T u1, T u2) {
+    const V3<T> none{0, 0, 0};
+    if (ul < m.p_glass) {
+        V3<T> h = vndf(m.alpha, wo, u1, u2);
+        T co = dot3(wo, h);
+        T F = fresnel_diel(co, m.eta);
+        if (ul < m.p_glass * F) {
+            V3<T> r = h * (T(2) * co) - wo;
+            return r.z > T(0) ? r : none;
+        }
+        T ie = T(1) / m.eta;
+        T s2 = ie * ie * std::max(T(0), T(1) - co * co);
+        T ct = std::sqrt(std::max(T(0), T(1) - s2));
+        V3<T> t = h * (ie * co - ct) - wo * ie;
+        return t.z < T(0) ? t : none;
+    }
+    ul -= m.p_glass;
+    if (ul < m.p_cc) {
+        T c2 = (T(1) - std::pow(m.cc_a2, T(1) - u1)) / (T(1) - m.cc_a2);
+        T ch = std::sqrt(std::min(std::max(c2, T(0)), T(1)));
+        T sh = std::sqrt(std::max(T(0), T(1) - ch * ch));
+        T phi = T(2 * M_PI) * u2;
+        V3<T> h{sh * std::cos(phi), sh * std::sin(phi), ch};
+        T d = dot3(wo, h);
+        if (d < T(0)) { h = -h; d = -d; }
+        V3<T> r = h * (T(2) * d) - wo;
+        return r.z > T(0) ? r : none;
+    }
+    ul -= m.p_cc;
+    const T rest = T(1) - m.p_glass - m.p_cc;
+    ul = rest > T(0) ? ul / rest : T(1);
+    V3<T> r;
+    if (ul < m.p_spec) {
+        V3<T> Ne = vndf(m.alpha, wo, u1, u2);
+        r = Ne * (T(2) * dot3(wo, Ne)) - wo;
+    } else {
+        T rr = std::sqrt(u1), phi = T(2 * M_PI) * u2;
+        r = {rr * std::cos(phi), rr * std::sin(phi), std::sqrt(std::max(T(0), T(1) - u1))};
+    }
+    return r.z > T(0) ? r : none;
 }
 template <class T> T power(T a, T b) {
     T a2 = a * a, b2 = b * b;
@@ -546,7 +659,8 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
                 for (int c2 = 0; c2 < 3; ++c2) sum[c2] += (double)at(thr, c2) * cache.rgb[c2];
                 break;
             }
-            if (dot3(ng, wo) < T(0)) ng = -ng;
+            const bool front = dot3(ng, wo) >= T(0);  // wo on the winding normal's side
+            if (!front) ng = -ng;
             // Shading normal: the interpolated vertex normal on ng's side when
             // wo lies above it, else ng (the device's shading_normal).
             V3<T> ns = ng;
@@ -572,7 +686,9 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
                 T tv = (T)uv[1] * w0 + (T)uv[3] * h.u + (T)uv[5] * h.v;
                 base = base * texture<T>(s, lut, m.base_texture, tu, tv);
             }
-            Mat<T> M = make_mat<T>(base, (T)m.metallic, (T)m.roughness, (T)m.specular);
+            Mat<T> M = make_mat<T>(base, (T)m.metallic, (T)m.roughness, (T)m.specular, (T)m.specular_tint,
+                                   (T)m.sheen, (T)m.sheen_tint, (T)m.clearcoat, (T)m.clearcoat_roughness,
+                                   (T)m.transmission, (T)m.ior, front);
             V3<T> Tt, Bt;
             basis(ns, Tt, Bt);
             V3<T> wol{dot3(wo, Tt), dot3(wo, Bt), dot3(wo, ns)};
@@ -587,15 +703,17 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
                 T pmf = (T)L.pmf;
                 V3<T> contrib{0, 0, 0}, wi{0, 0, 1};
                 T dist = 0;
+                bool below = false;  // light sample on the far side (glass lobe)
                 if (L.type == AQUA_LIGHT_POINT) {
                     V3<T> dl = lp - p;
                     T d2 = dot3(dl, dl);
                     dist = std::sqrt(d2);
                     wi = dl * (T(1) / dist);
                     T cs = dot3(wi, ns), cg = dot3(wi, ng);
-                    if (cs > T(0) && cg > T(0) && d2 > T(0)) {
+                    below = M.wglass > T(0) && cs < T(0) && cg < T(0);
+                    if (((cs > T(0) && cg > T(0)) || below) && d2 > T(0)) {
                         V3<T> wil{dot3(wi, Tt), dot3(wi, Bt), cs};
-                        contrib = thr * eval(M, wol, wil) * le * (cs / (d2 * pmf));
+                        contrib = thr * eval(M, wol, wil) * le * (std::fabs(cs) / (d2 * pmf));
                     }
                 } else {
                     V3<T> le1{(T)L.e1[0], (T)L.e1[1], (T)L.e1[2]}, le2{(T)L.e2[0], (T)L.e2[1], (T)L.e2[2]}, xl;
@@ -612,24 +730,26 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
                     dist = std::sqrt(d2);
                     wi = dl * (T(1) / dist);
                     T cl = -dot3(wi, nl), cs = dot3(wi, ns), cg = dot3(wi, ng);
-                    if (cl > T(0) && cs > T(0) && cg > T(0) && d2 > T(0)) {
+                    below = M.wglass > T(0) && cs < T(0) && cg < T(0);
+                    if (cl > T(0) && ((cs > T(0) && cg > T(0)) || below) && d2 > T(0)) {
                         V3<T> wil{dot3(wi, Tt), dot3(wi, Bt), cs};
                         T pl = pmf * d2 / (area * cl);
                         T w = power(pl, pdf(M, wol, wil));
-                        contrib = thr * eval(M, wol, wil) * le * (cs * w / pl);
+                        contrib = thr * eval(M, wol, wil) * le * (std::fabs(cs) * w / pl);
                     }
                 }
                 if (contrib.x > T(0) || contrib.y > T(0) || contrib.z > T(0)) {
                     st[2] += 1;
-                    Closest<T> o2 = closest<T>(s, offset(p, ng), wi, dist * T(1.0 - 1e-4), true);
+                    Closest<T> o2 = closest<T>(s, offset(p, below ? -ng : ng), wi, dist * T(1.0 - 1e-4), true);
                     if (!o2.hit) { sum[0] += contrib.x; sum[1] += contrib.y; sum[2] += contrib.z; }
                 }
             }
             V3<T> wil = sample(M, wol, u[3], u[4], u[5]);
-            if (!(wil.z > T(0) && wol.z > T(0))) break;
+            const bool through = wil.z < T(0);  // refracted by the glass lobe
+            if (!((wil.z > T(0) || through) && wol.z > T(0))) break;
             T pb = pdf(M, wol, wil);
             if (!(pb > T(0))) break;
-            thr = thr * eval(M, wol, wil) * (wil.z / pb);
+            thr = thr * eval(M, wol, wil) * (std::fabs(wil.z) / pb);
             if (!(max3(thr) > T(0)) || !std::isfinite(thr.x) || !std::isfinite(thr.y) || !std::isfinite(thr.z)) break;
             if (depth >= rr_depth) {
                 T q = std::min(T(1), max3(thr));
@@ -637,8 +757,12 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
                 thr = thr * (T(1) / q);
             }
             d = unit(Tt * wil.x + Bt * wil.y + ns * wil.z);
-            if (s->nrm && !(dot3(d, ng) > T(0))) break;  // below the geometric surface
-            o = offset(p, ng);
+            if (through) {
+                if (!(dot3(d, ng) < T(0))) break;  // refraction must cross the surface
+            } else if (s->nrm && !(dot3(d, ng) > T(0))) {
+                break;  // below the geometric surface
+            }
+            o = offset(p, through ? -ng : ng);
             pdf_b = pb;
         }
         st[0] += 1;
@@ -820,6 +944,32 @@ int orc_render(const orc_scene* s, int precision, int32_t spp, int32_t spp_offse
                              pixel_end, -1, nullptr, out, stats);
 }
 
+static Mat<double> mat_of(const aqua_material* m, int front) {
+    return make_mat<double>({m->base_color[0], m->base_color[1], m->base_color[2]}, m->metallic, m->roughness,
+                            m->specular, m->specular_tint, m->sheen, m->sheen_tint, m->clearcoat,
+                            m->clearcoat_roughness, m->transmission, m->ior, front != 0);
+}
+
+void orc_bsdf_eval(const aqua_material* m, int front, const double* wo, const double* wi, int64_t n, double* f,
+                   double* pdf_out) {
+    const Mat<double> M = mat_of(m, front);
+    for (int64_t k = 0; k < n; ++k) {
+        V3<double> o{wo[3 * k], wo[3 * k + 1], wo[3 * k + 2]}, i{wi[3 * k], wi[3 * k + 1], wi[3 * k + 2]};
+        V3<double> v = eval(M, o, i);
+        f[3 * k] = v.x; f[3 * k + 1] = v.y; f[3 * k + 2] = v.z;
+        if (pdf_out) pdf_out[k] = pdf(M, o, i);
+    }
+}
+
+void orc_bsdf_sample(const aqua_material* m, int front, const double* wo, const double* u, int64_t n, double* wi) {
+    const Mat<double> M = mat_of(m, front);
+    for (int64_t k = 0; k < n; ++k) {
+        V3<double> o{wo[3 * k], wo[3 * k + 1], wo[3 * k + 2]};
+        V3<double> v = sample(M, o, u[3 * k], u[3 * k + 1], u[3 * k + 2]);
+        wi[3 * k] = v.x; wi[3 * k + 1] = v.y; wi[3 * k + 2] = v.z;
+    }
+}
+
 uint32_t orc_pcg32_first(uint64_t initstate, uint64_t initseq, uint32_t* out, int n) {
     Pcg r;
     r.seed(initstate, initseq);
@@ -887,6 +1037,56 @@ void orc_trace_brute_f64(const orc_scene* s, const float* rays, int64_t n, doubl
     });
 }
 
+}  // extern "C"
+
+// Renders n pixels, pixel_of(k) for k in [0, n), writing pixel k's mean to
+// out_of(k)[0..2]; stats as orc_render.
+template <class PixelOf, class OutOf>
+static void render_pixel_set(const orc_scene* s, int precision, int32_t spp, int32_t spp_offset, int32_t max_depth,
+                             int32_t rr_depth, uint64_t seed, int threads, int64_t n, PixelOf pixel_of,
+                             OutOf out_of, const CacheConst& cache, double* stats) {
+    static const Lut lut;
+    std::vector<double> cdf((size_t)std::max(s->n_lights, 1));
+    double acc = 0;
+    for (int i = 0; i < s->n_lights; ++i) {
+        acc += (double)s->lights[i].pmf;
+        cdf[(size_t)i] = (i + 1 == s->n_lights) ? 1.0 : (double)(float)acc;
+    }
+    std::vector<double> st((size_t)n * 3, 0.0);
+    parallel_for(n, threads, [&](int64_t k) {
+        uint32_t pixel = pixel_of(k);
+        double sum[3] = {0, 0, 0};
+        double* sk = &st[3 * (size_t)k];
+        if (precision == 64)
+            render_pixel<double>(s, lut, cdf, spp, spp_offset, max_depth, rr_depth, seed, pixel, sum, sk, cache);
+        else
+            render_pixel<float>(s, lut, cdf, spp, spp_offset, max_depth, rr_depth, seed, pixel, sum, sk, cache);
+        float* o = out_of(k);
+        for (int c = 0; c < 3; ++c) o[c] = (float)(sum[c] / spp);
+    });
+    if (stats) {
+        stats[0] = stats[1] = stats[2] = 0;
+        for (int64_t k = 0; k < n; ++k)
+            for (int c = 0; c < 3; ++c) stats[c] += st[3 * (size_t)k + c];
+    }
+}
+
+extern "C" {
+
+int orc_render_pixels(const orc_scene* s, int precision, int32_t spp, int32_t spp_offset, int32_t max_depth,
+                      int32_t rr_depth, uint64_t seed, int threads, const uint32_t* pixels, int64_t n, float* out,
+                      double* stats) {
+    if (!s || (n > 0 && (!pixels || !out)) || n < 0 || spp <= 0 || (precision != 32 && precision != 64)) return 1;
+    const int64_t npix = (int64_t)s->cam.width * s->cam.height;
+    for (int64_t k = 0; k < n; ++k)
+        if ((int64_t)pixels[k] >= npix) return 1;
+    CacheConst cache;
+    cache.query_depth = -1;
+    render_pixel_set(s, precision, spp, spp_offset, max_depth, rr_depth, seed, threads, n,
+                     [&](int64_t k) { return pixels[k]; }, [&](int64_t k) { return out + 3 * k; }, cache, stats);
+    return 0;
+}
+
 int orc_render_cached(const orc_scene* s, int precision, int32_t spp, int32_t spp_offset, int32_t max_depth,
                       int32_t rr_depth, uint64_t seed, int threads, int64_t pixel_begin, int64_t pixel_end,
                       int32_t query_depth, const float* cache_rgb, float* out, double* stats) {
@@ -898,33 +1098,13 @@ int orc_render_cached(const orc_scene* s, int precision, int32_t spp, int32_t sp
     int64_t npix = (int64_t)s->cam.width * s->cam.height;
     pixel_begin = std::max<int64_t>(0, pixel_begin);
     pixel_end = std::min<int64_t>(npix, pixel_end);
-    if (pixel_end <= pixel_begin) return 0;
-    static const Lut lut;
-    std::vector<double> cdf((size_t)std::max(s->n_lights, 1));
-    // Light-selection CDF: running double sum of the float pmfs, stored as
-    // float, last entry 1 (the table the device searches).
-    double acc = 0;
-    for (int i = 0; i < s->n_lights; ++i) {
-        acc += (double)s->lights[i].pmf;
-        cdf[(size_t)i] = (i + 1 == s->n_lights) ? 1.0 : (double)(float)acc;
+    if (pixel_end <= pixel_begin) {
+        if (stats) stats[0] = stats[1] = stats[2] = 0;
+        return 0;
     }
-    int64_t n = pixel_end - pixel_begin;
-    std::vector<double> st((size_t)n * 3, 0.0);
-    parallel_for(n, threads, [&](int64_t k) {
-        uint32_t pixel = (uint32_t)(pixel_begin + k);
-        double sum[3] = {0, 0, 0};
-        double* sk = &st[3 * (size_t)k];
-        if (precision == 64)
-            render_pixel<double>(s, lut, cdf, spp, spp_offset, max_depth, rr_depth, seed, pixel, sum, sk, cache);
-        else
-            render_pixel<float>(s, lut, cdf, spp, spp_offset, max_depth, rr_depth, seed, pixel, sum, sk, cache);
-        for (int c = 0; c < 3; ++c) out[3 * (size_t)pixel + c] = (float)(sum[c] / spp);
-    });
-    if (stats) {
-        stats[0] = stats[1] = stats[2] = 0;
-        for (int64_t k = 0; k < n; ++k)
-            for (int c = 0; c < 3; ++c) stats[c] += st[3 * (size_t)k + c];
-    }
+    render_pixel_set(s, precision, spp, spp_offset, max_depth, rr_depth, seed, threads, pixel_end - pixel_begin,
+                     [&](int64_t k) { return (uint32_t)(pixel_begin + k); },
+                     [&](int64_t k) { return out + 3 * (size_t)(pixel_begin + k); }, cache, stats);
     return 0;
 }
 

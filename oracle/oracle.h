@@ -72,6 +72,12 @@ int orc_render(const orc_scene* s, int precision, int32_t spp, int32_t spp_offse
                int32_t rr_depth, uint64_t seed, int threads, int64_t pixel_begin, int64_t pixel_end,
                float* out, double* stats);
 
+/* As orc_render, for an arbitrary set of pixels: pixels[k] (each below
+ * width*height) is rendered into out[3k..3k+2]. Returns 1 on a bad index. */
+int orc_render_pixels(const orc_scene* s, int precision, int32_t spp, int32_t spp_offset, int32_t max_depth,
+                      int32_t rr_depth, uint64_t seed, int threads, const uint32_t* pixels, int64_t n, float* out,
+                      double* stats);
+
 /* As orc_render, with a constant radiance cache: every path stops at bounce
  * query_depth (0 = first hit) and adds throughput x cache_rgb there. */
 int orc_render_cached(const orc_scene* s, int precision, int32_t spp, int32_t spp_offset, int32_t max_depth,
@@ -93,6 +99,15 @@ void orc_mlp_grad(const float* w, const float* x, const float* target, int64_t n
                   double* grad, double* loss);
 /* Input encoding of raw vertex features (16 floats each) to 64 floats. */
 void orc_nrc_encode(const float* raw, int64_t n, const float* bmin, const float* bmax, float* x);
+
+/* The Principled BSDF of the path tracer in double precision, in the local
+ * shading frame (z = normal, wo.z > 0): f (3 values, not times cos) and the
+ * sampling pdf (solid angle) for n direction pairs, and n sampled
+ * directions from n triples of uniform numbers (wi.z < 0: refraction,
+ * wi.z == 0: no sample). front = wo on the side of the winding normal. */
+void orc_bsdf_eval(const aqua_material* m, int front, const double* wo, const double* wi, int64_t n, double* f,
+                   double* pdf);
+void orc_bsdf_sample(const aqua_material* m, int front, const double* wo, const double* u, int64_t n, double* wi);
 
 /* Reference values the tests print. */
 double orc_srgb_to_linear(double c);

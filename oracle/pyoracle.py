@@ -50,6 +50,11 @@ def lib():
         L.orc_render_cached.argtypes = [P, C.c_int, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
                                         C.c_int, C.c_int64, C.c_int64, C.c_int32, P, P, P]
         L.orc_render_cached.restype = C.c_int
+        L.orc_render_pixels.argtypes = [P, C.c_int, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
+                                        C.c_int, P, C.c_int64, P, P]
+        L.orc_render_pixels.restype = C.c_int
+        L.orc_bsdf_eval.argtypes = [P, C.c_int, P, P, C.c_int64, P, P]
+        L.orc_bsdf_sample.argtypes = [P, C.c_int, P, P, C.c_int64, P]
         L.orc_srgb_to_linear.argtypes = [C.c_double]
         L.orc_srgb_to_linear.restype = C.c_double
         L.orc_pcg32_first.argtypes = [C.c_uint64, C.c_uint64, P, C.c_int]
@@ -146,6 +151,47 @@ class OracleScene:
         if r != 0:
             raise RuntimeError("orc_render rejected its arguments")
         return out, stats
+
+    def render_pixels(self, pixels, spp: int, max_depth: int, seed: int = 0, precision: int = 64,
+                      rr_depth: int = 3, spp_offset: int = 0, threads: int = 0):
+        """Renders the listed pixel indices; returns (len(pixels) x 3, stats)."""
+        px = np.ascontiguousarray(pixels, np.uint32)
+        out = np.zeros((px.shape[0], 3), np.float32)
+        stats = np.zeros(3, np.float64)
+        r = lib().orc_render_pixels(C.byref(self.s), precision, spp, spp_offset, max_depth, rr_depth, seed, threads,
+                                    _p(px), px.shape[0], _p(out), _p(stats))
+        if r != 0:
+            raise RuntimeError("orc_render_pixels rejected its arguments")
+        return out, stats
+
+    def render_rows(self, rows, spp: int, max_depth: int, **kw):
+        """Renders whole image rows; returns (len(rows) x width x 3, stats)."""
+        rows = np.asarray(rows, np.int64)
+        px = (rows[:, None] * self.width + np.arange(self.width)[None, :]).reshape(-1)
+        out, st = self.render_pixels(px, spp, max_depth, **kw)
+        return out.reshape(rows.shape[0], self.width, 3), st
+
+
+def bsdf_eval(mat, wo, wi, front: bool = True):
+    """f (n x 3) and pdf (n) of the Principled BSDF for direction pairs in the
+    local frame; mat is an aqua.Material."""
+    wo = np.ascontiguousarray(wo, np.float64).reshape(-1, 3)
+    wi = np.ascontiguousarray(wi, np.float64).reshape(-1, 3)
+    wo = np.broadcast_to(wo, wi.shape).copy() if wo.shape[0] == 1 else wo
+    f = np.zeros(wi.shape, np.float64)
+    p = np.zeros(wi.shape[0], np.float64)
+    lib().orc_bsdf_eval(C.byref(mat), int(front), _p(wo), _p(wi), wi.shape[0], _p(f), _p(p))
+    return f, p
+
+
+def bsdf_sample(mat, wo, u, front: bool = True):
+    """Sampled directions (n x 3) for n x 3 uniform numbers."""
+    u = np.ascontiguousarray(u, np.float64).reshape(-1, 3)
+    wo = np.ascontiguousarray(wo, np.float64).reshape(-1, 3)
+    wo = np.broadcast_to(wo, u.shape).copy() if wo.shape[0] == 1 else wo
+    wi = np.zeros(u.shape, np.float64)
+    lib().orc_bsdf_sample(C.byref(mat), int(front), _p(wo), _p(u), u.shape[0], _p(wi))
+    return wi
 
 
 def srgb_to_linear(c: float) -> float:

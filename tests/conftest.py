@@ -47,6 +47,25 @@ def gpu_ctx(built):
     ctx.close()
 
 
+def reference_scene(name: str):
+    """Path of one of the reference project's scene files, or None.
+
+    Looked up in $AQUA_REFERENCE_DIR/scenes (a checkout of the reference),
+    then in tests/golden/reference_scenes (the staged living-room copy, see
+    tests/golden/stage_reference_scenes.py), then in tests/golden/cbox (the
+    committed Cornell scene)."""
+    dirs = []
+    env = os.environ.get("AQUA_REFERENCE_DIR")
+    if env:
+        dirs.append(os.path.join(env, "scenes"))
+    dirs += [os.path.join(GOLDEN, "reference_scenes"), os.path.join(GOLDEN, "cbox")]
+    for d in dirs:
+        p = os.path.join(d, name)
+        if os.path.exists(p):
+            return p
+    return None
+
+
 def aqua_host_only() -> int:
     return -2  # AQUA_DEVICE_HOST_ONLY
 

@@ -84,4 +84,7 @@ def main(ref: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AQUA_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: make_reference_facts.py <reference checkout> (or set AQUA_REFERENCE_DIR)")
+    main(ref)

@@ -49,14 +49,14 @@ def test_binding_declares_every_symbol():
 def test_struct_layouts():
     assert ctypes.sizeof(aqua.Ray) == 32
     assert ctypes.sizeof(aqua.Hit) == 16
-    assert ctypes.sizeof(aqua.Material) == 32
+    assert ctypes.sizeof(aqua.Material) == 64
     assert ctypes.sizeof(aqua.Light) == 56
-    assert ctypes.sizeof(aqua.IntegratorCfg) == 56
+    assert ctypes.sizeof(aqua.IntegratorCfg) == 64
 
 
 def test_status_strings_and_version():
     lib = aqua.load_library()
-    assert lib.aqua_version() == 200  # four-wide BVH export layout
+    assert lib.aqua_version() == 300  # 64-byte aqua_material with the Principled lobes
     assert lib.aqua_status_string(0) == b"ok"
     assert lib.aqua_status_string(4) == b"missing asset"
     assert lib.aqua_status_string(99) == b"unknown status"

@@ -281,3 +281,28 @@ def test_allocation_failure_is_reported():
             c.render(s, c.integrator(spp=1))
         assert e.value.status == aqua.ERR_OOM
         s.free()
+
+
+def test_row_subset_equals_rows_of_the_full_image(gpu_ctx):
+    """With row_step > 1 only every row_step-th row is rendered, and each
+    pixel keeps its full-image random-number stream: the rows equal the same
+    rows of a full render bit for bit (one slot per pixel on both sides)."""
+    import aqua
+
+    s = gpu_ctx.procedural(3, seed=0, width=96, height=54)
+    cfg = gpu_ctx.integrator(spp=8, max_depth=8, rr_depth=3, seed=4)
+    one = gpu_ctx.tuning(replicas=1)
+    full, _ = gpu_ctx.render(s, cfg, tuning=one)
+    for begin, step in [(0, 2), (3, 7), (5, 16)]:
+        rows = np.arange(begin, 54, step)
+        sub = gpu_ctx.integrator(spp=8, max_depth=8, rr_depth=3, seed=4, row_begin=begin, row_step=step)
+        out = np.zeros((len(rows), 96, 3), np.float32)
+        img, st = gpu_ctx.render(s, sub, tuning=one, out=out)
+        assert st.paths == len(rows) * 96 * 8
+        assert np.array_equal(img, full[rows])
+        auto, _ = gpu_ctx.render(s, sub, out=np.zeros_like(out))  # sample replicas on the small film
+        np.testing.assert_allclose(auto, full[rows], rtol=1e-5, atol=1e-6)
+    bad = gpu_ctx.integrator(spp=1, max_depth=2, row_begin=4, row_step=3)
+    with pytest.raises(aqua.AquaError):
+        gpu_ctx.render(s, bad)
+    s.free()

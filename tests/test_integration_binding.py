@@ -1,4 +1,4 @@
-"""The Rust binding in INTEGRATION.md (the `src/ffi.rs` a maintainer of the
+"""The Rust binding rust/src/ffi.rs (the `src/ffi.rs` a maintainer of the
 reference crate adds) against include/aqua.h, and the ctypes binding's struct
 layouts against the header. No Rust compiler exists here, so the check is
 textual: every entry point with the same parameter and return types (pointer
@@ -16,7 +16,7 @@ import aqua
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "aqua.h")
-DOC = os.path.join(ROOT, "INTEGRATION.md")
+FFI = os.path.join(ROOT, "rust", "src", "ffi.rs")
 
 # scalar spellings -> one canonical name per ABI type
 C_BASE = {"int32_t": "i32", "int": "i32", "aqua_status": "i32", "uint32_t": "u32", "uint64_t": "u64",
@@ -95,9 +95,9 @@ def c_constants() -> dict:
 
 # ---------------------------------------------------------------- Rust side
 def rust_text() -> str:
-    blocks = re.findall(r"```rust\n(.*?)```", open(DOC).read(), flags=re.S)
+    blocks = [open(FFI).read()]
     ffi = [b for b in blocks if 'extern "C"' in b and "pub struct aqua_stats" in b]
-    assert len(ffi) == 1, "INTEGRATION.md holds exactly one complete ffi.rs block"
+    assert len(ffi) == 1, "rust/src/ffi.rs is the complete binding"
     return re.sub(r"//[^\n]*", " ", ffi[0])
 
 

@@ -22,8 +22,10 @@ import pytest
 import aqua
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-TEXTURES = "/root/reference/scenes/textures"
-need_ref = pytest.mark.skipif(not os.path.isdir(TEXTURES), reason="reference textures not mounted")
+from conftest import reference_scene
+
+TEXTURES = reference_scene("textures")
+need_ref = pytest.mark.skipif(TEXTURES is None, reason="reference textures not staged")
 
 # ---------------------------------------------------------------- encoder
 ZZ = []

@@ -18,9 +18,13 @@ import pytest
 import aqua
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REF_SCENES = "/root/reference/scenes"
+from conftest import reference_scene
+
+REF_SCENES = os.path.dirname(reference_scene("cbox.json") or "")
+ROOM = reference_scene("room.json")
 FACTS = json.load(open(os.path.join(GOLDEN, "reference_facts.json")))
-need_ref = pytest.mark.skipif(not os.path.isdir(REF_SCENES), reason="reference scenes not mounted")
+need_ref = pytest.mark.skipif(not REF_SCENES, reason="reference Cornell scene not found")
+need_room = pytest.mark.skipif(ROOM is None, reason="reference living-room scene not staged")
 
 
 # ---------------------------------------------------------------- BSON writer
@@ -334,19 +338,19 @@ def test_reference_cbox(host_ctx):
     s.free()
 
 
-@need_ref
+@need_room
 def test_reference_room(host_ctx):
     with pytest.raises(aqua.AquaError) as e:
-        host_ctx.load_scene(os.path.join(REF_SCENES, "room.json"))
+        host_ctx.load_scene(ROOM)
     assert e.value.status in (aqua.ERR_UNSUPPORTED, aqua.ERR_MISSING_ASSET)
-    s = host_ctx.load_scene(os.path.join(REF_SCENES, "room.json"), allow_missing=True)
+    s = host_ctx.load_scene(ROOM, allow_missing=True)
     i = s.info()
     f = FACTS["room"]
     assert i.num_triangles == f["triangles_present"] == 394269
     assert i.num_meshes == f["meshes_present"] == 152
     assert [i.width, i.height] == f["res"]
     # Every `Image` texture is decoded (JPEG), once per file.
-    room = json.load(open(os.path.join(REF_SCENES, "room.json")))
+    room = json.load(open(ROOM))
     images = set()
 
     def walk(x):

@@ -19,8 +19,12 @@ import pytest
 
 import aqua
 
-REF_SCENES = "/root/reference/scenes"
-need_ref = pytest.mark.skipif(not os.path.isdir(REF_SCENES), reason="reference scenes not mounted")
+from conftest import reference_scene
+
+REF_SCENES = os.path.dirname(reference_scene("cbox.json") or "")
+ROOM = reference_scene("room.json")
+need_ref = pytest.mark.skipif(not REF_SCENES, reason="reference Cornell scene not found")
+need_room = pytest.mark.skipif(ROOM is None, reason="reference living-room scene not staged")
 
 
 def read_bson(b: bytes):

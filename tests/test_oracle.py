@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import pyoracle
-from conftest import random_rays
+from conftest import random_rays, reference_scene
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 FACTS = json.load(open(os.path.join(GOLDEN, "reference_facts.json")))
@@ -139,13 +139,13 @@ def test_encoding_shape_and_ranges():
     np.testing.assert_allclose(x[:, 0:48:2] ** 2 + x[:, 1:48:2] ** 2, 1.0, atol=1e-6)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/scenes"), reason="reference scenes not mounted")
+@pytest.mark.skipif(reference_scene("room.json") is None, reason="reference living-room scene not staged")
 def test_bvh_walk_equals_brute_force_reference_room(host_ctx):
     """The reference's own living-room geometry (room.json, 394,269 triangles
     from 152 BSON meshes): the four-wide BVH walk finds exactly the brute-force
     closest hits for rays from the camera and from random points inside the
     room, closest and any hit."""
-    s = host_ctx.load_scene("/root/reference/scenes/room.json", allow_missing=True)
+    s = host_ctx.load_scene(reference_scene("room.json"), allow_missing=True)
     o = pyoracle.OracleScene.from_aqua(s)
     verts = s.triangles()[0].reshape(-1, 3)
     lo, hi = verts.min(0), verts.max(0)
@@ -163,3 +163,15 @@ def test_bvh_walk_equals_brute_force_reference_room(host_ctx):
     occ = o.trace_bvh_f32(rays, any_hit=True)[3]
     assert np.array_equal(occ >= 0, pb >= 0)
     s.free()
+
+
+def test_render_pixel_list_equals_full_render(cornell_orc):
+    """The pixel-list render (every k-th row, used for uniform row samples of
+    large images) gives each pixel exactly what the full render gives it."""
+    full, st = cornell_orc.render(8, 8, seed=3, precision=32)
+    rows = [0, 5, 17, 31]
+    part, pst = cornell_orc.render_rows(rows, 8, 8, seed=3, precision=32)
+    assert np.array_equal(part, full[rows])
+    assert 0 < pst[0] == 8 * 32 * len(rows) < st[0]
+    with pytest.raises(RuntimeError):
+        cornell_orc.render_pixels([32 * 32], 1, 1)

@@ -10,7 +10,11 @@ compares each image with the one aqua_render returns for the same inputs,
 within the tests' image tolerance (relMSE 1e-3; the two are in fact
 bit-identical, because every pixel's samples run in the same order whatever
 the slot count). It also checks that the call allocated no workspace and that
-an image above the fixed limit is refused before any device work. The file is
+an image above the fixed limit is refused before any device work. A 512x512
+image (262,144 pixels over 65,536 path slots, so each slot owns four pixels)
+is compared with the FP64 oracle at the same seed and with aqua_render, and
+depth limits outside [0, 250] are refused like aqua_render refuses them. The
+file is
 named so that pytest collects it last, and it builds its own context so it
 passes alone in a fresh process as well as after the other tests.
 """
@@ -77,4 +81,57 @@ def test_noalloc_refuses_images_above_the_limit():
                                              ctypes.c_void_p(out.data_ptr()), None)
         assert status == aqua.ERR_INVALID_ARG
         assert b"scratch limit" in ctx.lib.aqua_last_error(ctx.handle)
+        scene.free()
+
+
+def test_noalloc_several_pixels_per_slot_against_the_oracle():
+    """512x512 = 2^18 pixels on 2^16 slots: slot s runs pixels s, s + 2^16,
+    s + 2^17 and s + 3 * 2^16 in turn. Sample-matched (same seed, same PCG32
+    stream per pixel) against the FP64 oracle, and bit-equal to aqua_render
+    with one replica."""
+    torch = pytest.importorskip("torch")
+    import aqua
+    import pyoracle
+
+    w = h = 512
+    spp = 2
+    with aqua.Context(device=0) as ctx:
+        lib = ctx.lib
+        scene = ctx.procedural(2, seed=0, width=w, height=h)
+        cfg = ctx.integrator(spp=spp, max_depth=8, rr_depth=3, seed=5)
+        out = torch.full((h * w * 3,), -1.0, dtype=torch.float32, device="cuda:0")
+        torch.cuda.synchronize()
+        st = aqua.Stats()
+        status = lib.aqua_render_noalloc(ctx.handle, scene.handle, ctypes.byref(cfg),
+                                         ctypes.c_void_p(out.data_ptr()), ctypes.byref(st))
+        assert status == aqua.OK, lib.aqua_last_error(ctx.handle)
+        assert st.paths == w * h * spp
+        img = out.cpu().numpy().reshape(h, w, 3)
+        assert np.isfinite(img).all()
+        o = pyoracle.OracleScene.from_aqua(scene)
+        ref, ost = o.render(spp, 8, seed=5, precision=64)
+        assert rel_mse(img, ref) < TOL
+        assert abs(st.ext_rays - ost[1]) / ost[1] < 2e-3
+        assert abs(st.shadow_rays - ost[2]) / ost[2] < 2e-3
+        again, _ = ctx.render(scene, cfg, tuning=ctx.tuning(replicas=1))
+        assert np.array_equal(img, again)
+        scene.free()
+
+
+@pytest.mark.parametrize("max_depth,rr_depth", [(251, 3), (-1, 3), (8, -1), (8, 251)])
+def test_noalloc_refuses_depths_out_of_range(max_depth, rr_depth):
+    torch = pytest.importorskip("torch")
+    import aqua
+
+    with aqua.Context(device=0) as ctx:
+        scene = ctx.procedural(1, seed=0, width=16, height=16)
+        cfg = ctx.integrator(spp=1, max_depth=max_depth, rr_depth=rr_depth, seed=0)
+        out = torch.zeros(16 * 16 * 3, dtype=torch.float32, device="cuda:0")
+        status = ctx.lib.aqua_render_noalloc(ctx.handle, scene.handle, ctypes.byref(cfg),
+                                             ctypes.c_void_p(out.data_ptr()), None)
+        assert status == aqua.ERR_INVALID_ARG
+        assert b"_depth must be in [0, 250]" in ctx.lib.aqua_last_error(ctx.handle)
+        # aqua_render refuses the same settings.
+        with pytest.raises(aqua.AquaError):
+            ctx.render(scene, cfg)
         scene.free()
