@@ -81,6 +81,7 @@ class Tuning(C.Structure):
 
 
 KERNEL_WAVEFRONT, KERNEL_PERSISTENT = 0, 1
+BVH_AUTO, BVH_FULL, BVH_QUANTIZED = -1, 0, 1
 
 
 class Stats(C.Structure):
@@ -98,7 +99,7 @@ class SceneInfo(C.Structure):
                 ("num_materials", C.c_int32), ("num_lights", C.c_int32), ("num_textures", C.c_int32),
                 ("num_meshes", C.c_int32), ("num_bvh_nodes", C.c_int32), ("bvh_depth", C.c_int32),
                 ("max_leaf_size", C.c_int32), ("device_bytes", C.c_uint64), ("upload_bytes", C.c_uint64),
-                ("env", C.c_float * 3), ("reserved", C.c_int32)]
+                ("env", C.c_float * 3), ("bvh_format", C.c_int32)]
 
 
 class Camera(C.Structure):
@@ -149,6 +150,8 @@ SIGNATURES = [
     ("aqua_scene_export_lights", C.c_int, [_P, _P, _P]),
     ("aqua_scene_export_texture", C.c_int, [_P, _P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P]),
     ("aqua_scene_export_bvh", C.c_int, [_P, _P, _P, _P]),
+    ("aqua_scene_export_bvh_quantized", C.c_int, [_P, _P, _P]),
+    ("aqua_scene_set_bvh_format", C.c_int, [_P, _P, C.c_int32]),
     ("aqua_load_integrator_json", C.c_int, [_P, C.c_char_p, C.POINTER(IntegratorCfg)]),
     ("aqua_integrator_defaults", None, [C.POINTER(IntegratorCfg)]),
     ("aqua_tuning_defaults", None, [C.POINTER(Tuning)]),
@@ -247,6 +250,15 @@ class Nrc:
     def encode_device(self, raw_ptr: int, n: int, x_ptr: int):
         self.ctx._check(self.ctx.lib.aqua_nrc_encode(self.ctx.handle, self.handle, C.c_void_p(raw_ptr), n,
                                                      C.c_void_p(x_ptr), 1))
+
+    def train_step_device(self, x_ptr: int, target_ptr: int, n: int) -> float:
+        """One Adam step on device buffers (x: n x 64 bf16, target: n x 3
+        fp32); returns the step's device milliseconds (CUDA events)."""
+        self.ctx._check(self.ctx.lib.aqua_nrc_train_step(self.ctx.handle, self.handle, C.c_void_p(x_ptr),
+                                                         C.c_void_p(target_ptr), n, None, 3))
+        ms = C.c_float()
+        self.ctx._check(self.ctx.lib.aqua_nrc_last_ms(self.ctx.handle, self.handle, C.byref(ms)))
+        return ms.value
 
     def forward(self, x_bf16: np.ndarray) -> np.ndarray:
         x = np.ascontiguousarray(x_bf16, np.uint16).reshape(-1, 64)
@@ -354,6 +366,16 @@ class Scene:
         self.ctx._check(self.ctx.lib.aqua_scene_export_texture(self.ctx.handle, self.handle, i, None, None,
                                                                _ptr(a)))
         return a
+
+    def bvh_quantized(self) -> np.ndarray:
+        """The quantized copy of the BVH, 16 floats per node."""
+        inf = self.info()
+        nodes = np.zeros((inf.num_bvh_nodes, 16), np.float32)
+        self.ctx._check(self.ctx.lib.aqua_scene_export_bvh_quantized(self.ctx.handle, self.handle, _ptr(nodes)))
+        return nodes
+
+    def set_bvh_format(self, fmt: int):
+        self.ctx._check(self.ctx.lib.aqua_scene_set_bvh_format(self.ctx.handle, self.handle, fmt))
 
     def bvh(self):
         """(nodes, tri_order): the four-wide BVH, 32 floats per node."""

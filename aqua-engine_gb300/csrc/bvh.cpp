@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cfloat>
 #include <cstring>
 #include <future>
@@ -307,6 +308,80 @@ FlatBvh build_bvh(const float* verts, size_t num_tris) {
     out.max_stack = max_stack;
     out.depth = max_depth;
     out.max_leaf = max_leaf;
+    return out;
+}
+
+// ------------------------------------------------------------------ quantized copy
+namespace {
+float scale_of(int e) {  // 2^(e - 127), e in [1, 254]
+    uint32_t b = (uint32_t)e << 23;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+// The plane a byte decodes to, exactly as the device computes it.
+float decode_plane(int q, float s, float o) { return std::fmaf((float)q, s, o); }
+}  // namespace
+
+std::vector<float> quantize_bvh(const FlatBvh& bvh) {
+    const int nn = bvh.num_nodes();
+    std::vector<float> out((size_t)kBvhQNodeFloats * (size_t)nn, 0.0f);
+    for (int k = 0; k < nn; ++k) {
+        const float* w = &bvh.nodes[(size_t)kBvhNodeFloats * (size_t)k];
+        int32_t link[4], count[4];
+        memcpy(link, &w[24], 16);
+        memcpy(count, &w[28], 16);
+        float* q = &out[(size_t)kBvhQNodeFloats * (size_t)k];
+        uint32_t bytes[6] = {0, 0, 0, 0, 0, 0};  // qlo.x, qhi.x, qlo.y, qhi.y, qlo.z, qhi.z
+        uint32_t exps = 0, counts = 0;
+        for (int a = 0; a < 3; ++a) {
+            float lo = std::numeric_limits<float>::infinity(), hi = -lo;
+            for (int c = 0; c < 4; ++c) {
+                if (link[c] == ~0) continue;
+                lo = std::min(lo, w[8 * a + c]);
+                hi = std::max(hi, w[8 * a + 4 + c]);
+            }
+            if (!(lo <= hi)) lo = hi = 0.0f;  // no children (not produced by the builder)
+            const float o = lo;
+            // Smallest power-of-two step whose 255 steps reach the far side,
+            // then the next ones while some child's plane does not fit.
+            int e = 1;
+            while (e < 254 && (double)scale_of(e) * 255.0 < (double)hi - (double)o) ++e;
+            for (;; ++e) {
+                const float sc = scale_of(e);
+                bool fits = true;
+                uint32_t blo = 0, bhi = 0;
+                for (int c = 0; c < 4 && fits; ++c) {
+                    int ql = 255, qh = 0;  // empty slot: skipped by its link
+                    if (link[c] != ~0) {
+                        const float clo = w[8 * a + c], chi = w[8 * a + 4 + c];
+                        ql = (int)std::floor(((double)clo - (double)o) / (double)sc);
+                        ql = std::max(0, std::min(255, ql));
+                        while (ql > 0 && decode_plane(ql, sc, o) > clo) --ql;
+                        qh = (int)std::ceil(((double)chi - (double)o) / (double)sc);
+                        qh = std::max(0, qh);
+                        while (qh <= 255 && decode_plane(qh, sc, o) < chi) ++qh;
+                        if (qh > 255 || decode_plane(ql, sc, o) > clo) fits = false;
+                    }
+                    blo |= (uint32_t)ql << (8 * c);
+                    bhi |= (uint32_t)std::min(qh, 255) << (8 * c);
+                }
+                if (fits || e >= 254) {
+                    bytes[2 * a] = blo;
+                    bytes[2 * a + 1] = bhi;
+                    exps |= (uint32_t)e << (8 * a);
+                    q[a] = o;
+                    break;
+                }
+            }
+        }
+        for (int c = 0; c < 4; ++c) counts |= (uint32_t)(count[c] & 0xff) << (8 * c);
+        memcpy(&q[3], &exps, 4);
+        memcpy(&q[4], link, 16);
+        memcpy(&q[8], bytes, 16);
+        memcpy(&q[12], &bytes[4], 8);
+        memcpy(&q[14], &counts, 4);
+    }
     return out;
 }
 

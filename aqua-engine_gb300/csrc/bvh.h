@@ -22,6 +22,20 @@
 // child = ~0, a leaf of no triangles. Node 0 is the root; nodes are numbered
 // depth first, children in slot order.
 //
+// Quantized node layout (the same tree, 64 bytes = four 16-byte words; after
+// Ylitie, Karras and Laine 2017, "Efficient Incoherent Ray Traversal on
+// GPUs Through Compressed Wide BVHs"): the children's boxes as 8-bit
+// offsets in a per-node frame,
+//   q0 = (origin.xyz as float, exponents ex | ey << 8 | ez << 16)
+//   q1 = (child0..3 as int32, the same links as w6)
+//   q2 = (qlo.x, qhi.x, qlo.y, qhi.y), q3 = (qlo.z, qhi.z, counts, 0), each
+//        a 32-bit word holding one byte per child (child k in byte k).
+// A plane decodes as fmaf(q, 2^(e - 127), origin) in float; the builder picks
+// every q so that the decoded box contains the child's box (it evaluates the
+// same fmaf), so a ray that hits a child's box hits its decoded box and the
+// walk finds the same closest hit. Empty slots have child = ~0 and are
+// skipped by the link, not by the box. Counts byte k = leaf size of child k.
+//
 // Triangle layout (leaf order): three 16-byte words per triangle,
 //   t0 = (v0.xyz, scene index as int bits)
 //   t1 = (v1.xyz, material | (light + 1) << 16 as int bits)
@@ -37,6 +51,7 @@ namespace aq {
 constexpr int kBvhMaxLeaf = 4;
 constexpr int kBvhWidth = 4;
 constexpr int kBvhNodeFloats = 32;   // 128-byte node
+constexpr int kBvhQNodeFloats = 16;  // 64-byte quantized node
 constexpr int kBvhStackSize = 96;    // traversal stack entries per ray
 
 struct FlatBvh {
@@ -51,5 +66,9 @@ struct FlatBvh {
 
 // verts: 9 floats per triangle.
 FlatBvh build_bvh(const float* verts, size_t num_tris);
+
+// The quantized copy of a built tree, kBvhQNodeFloats per node (same node
+// numbering and links).
+std::vector<float> quantize_bvh(const FlatBvh& bvh);
 
 }  // namespace aq

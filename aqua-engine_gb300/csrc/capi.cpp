@@ -74,18 +74,28 @@ void scene_release(aqua_scene* s) {
 }
 
 // Device image: nodes | triangle words | uvs | materials | lights | textures | texels.
-void scene_build_device(aqua_ctx* ctx, aqua_scene* s) {
+void scene_build_device(aqua_ctx* ctx, aqua_scene* s, bool rebuild_bvh) {
     const HostScene& h = s->host;
     size_t nt = h.num_tris();
     if (h.mats.size() > 65535) throw Error(AQUA_ERR_UNSUPPORTED, "more than 65535 materials");
     if (h.lights.size() > 65534) throw Error(AQUA_ERR_UNSUPPORTED, "more than 65534 lights");
     if (nt >= (1u << 28)) throw Error(AQUA_ERR_UNSUPPORTED, "more than 2^28 triangles");
-    s->bvh = build_bvh(h.verts.data(), nt);
-    if (s->bvh.max_stack >= kBvhStackSize) throw Error(AQUA_ERR_UNSUPPORTED, "BVH deeper than the traversal stack");
+    if (rebuild_bvh || s->bvh.nodes.empty()) {
+        s->bvh = build_bvh(h.verts.data(), nt);
+        if (s->bvh.max_stack >= kBvhStackSize)
+            throw Error(AQUA_ERR_UNSUPPORTED, "BVH deeper than the traversal stack");
+        s->qnodes = quantize_bvh(s->bvh);
+    }
     size_t nn = (size_t)s->bvh.num_nodes();
+    // Quantized nodes when asked, or (automatic) when the full-precision
+    // nodes would not stay cache resident: half the bytes per visit for the
+    // memory-bound walks, a few more instructions for the cache-bound ones.
+    const bool use_q = s->bvh_format == AQUA_BVH_QUANTIZED ||
+                       (s->bvh_format == AQUA_BVH_AUTO && nn * sizeof(float) * kBvhNodeFloats > kQuantizeAbove);
+    const size_t node_floats = use_q ? kBvhQNodeFloats : kBvhNodeFloats;
     size_t texels = 0;
     for (auto& t : h.textures) texels += (size_t)t.w * (size_t)t.h;
-    size_t o_nodes = 0, o_tris = align256(o_nodes + sizeof(float) * kBvhNodeFloats * nn), o_uvs = align256(o_tris + 48 * nt),
+    size_t o_nodes = 0, o_tris = align256(o_nodes + sizeof(float) * node_floats * nn), o_uvs = align256(o_tris + 48 * nt),
            o_mats = align256(o_uvs + 24 * nt), o_lights = align256(o_mats + 32 * h.mats.size()),
            o_texs = align256(o_lights + 64 * h.lights.size()),
            o_texels = align256(o_texs + 16 * h.textures.size()), o_nrm = align256(o_texels + 4 * texels),
@@ -105,7 +115,7 @@ void scene_build_device(aqua_ctx* ctx, aqua_scene* s) {
     }
     char* p = (char*)s->pinned;
     memset(p, 0, total);
-    memcpy(p + o_nodes, s->bvh.nodes.data(), sizeof(float) * kBvhNodeFloats * nn);
+    memcpy(p + o_nodes, use_q ? s->qnodes.data() : s->bvh.nodes.data(), sizeof(float) * node_floats * nn);
     float* tw = (float*)(p + o_tris);
     float* uw = (float*)(p + o_uvs);
     float* nw = h.nrm.empty() ? nullptr : (float*)(p + o_nrm);
@@ -166,12 +176,14 @@ void scene_build_device(aqua_ctx* ctx, aqua_scene* s) {
         off += (uint32_t)(h.textures[i].w * h.textures[i].h);
     }
     s->bytes = total;
+    s->bvh_format_used = use_q ? AQUA_BVH_QUANTIZED : AQUA_BVH_FULL;
     if (ctx->host_only) return;  // host-only context: no device image
     dev_free(s->dev);
     dev_alloc(ctx, s->dev, total);
     char* d = (char*)s->dev.ptr;
     DevScene& ds = s->ds;
     ds.nodes = (const float4*)(d + o_nodes);
+    ds.qbvh = use_q ? 1 : 0;
     ds.tris = (const float4*)(d + o_tris);
     ds.uvs = (const float2*)(d + o_uvs);
     ds.mats = (const DevMaterial*)(d + o_mats);
@@ -430,6 +442,7 @@ AQUA_API aqua_status aqua_scene_get_info(aqua_ctx* ctx, const aqua_scene* s, aqu
         out->device_bytes = s->dev.bytes;
         out->upload_bytes = s->bytes;
         for (int i = 0; i < 3; ++i) out->env[i] = s->host.env[i];
+        out->bvh_format = s->bvh_format_used;
     });
 }
 
@@ -518,6 +531,23 @@ AQUA_API aqua_status aqua_scene_export_normals(aqua_ctx* ctx, const aqua_scene* 
         need(s != nullptr, "scene is NULL");
         if (present) *present = s->host.nrm.empty() ? 0 : 1;
         if (nrm && !s->host.nrm.empty()) memcpy(nrm, s->host.nrm.data(), 4 * s->host.nrm.size());
+    });
+}
+
+AQUA_API aqua_status aqua_scene_export_bvh_quantized(aqua_ctx* ctx, const aqua_scene* s, float* nodes) {
+    return guard(ctx, [&]() {
+        need(s != nullptr, "scene is NULL");
+        if (nodes) memcpy(nodes, s->qnodes.data(), 4 * s->qnodes.size());
+    });
+}
+
+AQUA_API aqua_status aqua_scene_set_bvh_format(aqua_ctx* ctx, aqua_scene* s, int32_t format) {
+    return guard(ctx, [&]() {
+        need(s != nullptr, "scene is NULL");
+        need(format == AQUA_BVH_AUTO || format == AQUA_BVH_FULL || format == AQUA_BVH_QUANTIZED,
+             "format must be an AQUA_BVH_* value");
+        s->bvh_format = format;
+        scene_build_device(ctx, s, false);
     });
 }
 
@@ -916,7 +946,13 @@ AQUA_API aqua_status aqua_nrc_train_step(aqua_ctx* ctx, aqua_nrc* n, const uint1
         } else {
             need(((uintptr_t)x & 15) == 0, "x must be 16-byte aligned");
         }
+        std::unique_ptr<EventPair> ev;
+        if (flags & AQUA_NRC_TIMING) {
+            ev.reset(new EventPair());
+            AQ_CUDA(cudaEventRecord(ev->e[0], ctx->stream));
+        }
         nrc_train_step_dev(ctx, n->net, d_x, d_t, (int)cnt);
+        if (ev) AQ_CUDA(cudaEventRecord(ev->e[1], ctx->stream));
         struct {
             double loss;
             uint32_t tc_err, pad;
@@ -924,6 +960,7 @@ AQUA_API aqua_status aqua_nrc_train_step(aqua_ctx* ctx, aqua_nrc* n, const uint1
         AQ_CUDA(cudaMemcpyAsync(&rb, n->net.loss, 16, cudaMemcpyDeviceToHost, ctx->stream));
         AQ_CUDA(cudaStreamSynchronize(ctx->stream));
         if (rb.tc_err) nrc_check_tc(ctx, n->net);  // resets the flag and throws
+        if (ev) n->last_ms = ev->ms();
         const double l = rb.loss;
         if (loss) *loss = l / (double)(cnt * kNrcOut);
     });

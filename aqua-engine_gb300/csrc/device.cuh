@@ -32,7 +32,7 @@ struct DevCamera {
     int32_t width, height;
 };
 struct DevScene {
-    const float4* __restrict__ nodes;  // 8 words per four-wide node (bvh.h)
+    const float4* __restrict__ nodes;  // 8 words per four-wide node, or 4 per quantized node (bvh.h)
     const float4* __restrict__ tris;   // 3 words per triangle, leaf order
     const float2* __restrict__ uvs;    // 3 per triangle, leaf order
     const DevMaterial* __restrict__ mats;
@@ -45,6 +45,7 @@ struct DevScene {
     // sets any of those lobes (the base-model kernels run then).
     const float4* __restrict__ mext;
     int32_t n_nodes, n_tris, n_mats, n_lights, n_texs;
+    int32_t qbvh;  // 1: `nodes` holds quantized 64-byte nodes
     float env[3];
     DevCamera cam;
 };
@@ -118,6 +119,57 @@ __device__ __forceinline__ int32_t visit_wide(const DevScene& S, int32_t node, c
     return sp > 0 ? stack[--sp] : kTraversalDone;
 }
 
+// Plane of child byte k of a quantized word: fmaf(q, scale, origin), the
+// byte turned into a float exactly by placing it under the exponent of 2^23
+// (one byte permute and one subtraction).
+__device__ __forceinline__ float qplane(uint32_t word, int k, float scale, float origin) {
+    // result bytes: word byte k, zero, zero, 0x4B  ->  2^23 + q
+    const float q = __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7540u | (uint32_t)k)) - 8388608.0f;
+    return fmaf(q, scale, origin);
+}
+
+// visit_wide on a quantized 64-byte node (two 256-bit loads): the child
+// planes are decoded (bvh.h) and tested with the same slab_entry; empty
+// slots (link ~0) are skipped. Ordering, pushes and the result are those of
+// visit_wide.
+__device__ __forceinline__ int32_t visit_quantized(const DevScene& S, int32_t node, const RayPre& rp, float tfar,
+                                                   int32_t* stack, int& sp) {
+    const float4* np = S.nodes + 4 * (size_t)node;
+    float4 w0, w1, w2, w3;
+    ldg2x4(np, w0, w1);
+    ldg2x4(np + 2, w2, w3);
+    const uint32_t ex = __float_as_uint(w0.w);
+    const float sx = __uint_as_float((ex & 0xffu) << 23), sy = __uint_as_float(((ex >> 8) & 0xffu) << 23),
+                sz = __uint_as_float(((ex >> 16) & 0xffu) << 23);
+    const uint32_t lx = __float_as_uint(w2.x), hx = __float_as_uint(w2.y), ly = __float_as_uint(w2.z),
+                   hy = __float_as_uint(w2.w), lz = __float_as_uint(w3.x), hz = __float_as_uint(w3.y);
+    int32_t c0 = __float_as_int(w1.x), c1 = __float_as_int(w1.y), c2 = __float_as_int(w1.z),
+            c3 = __float_as_int(w1.w);
+    float t[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        t[k] = slab_entry(qplane(lx, k, sx, w0.x), qplane(hx, k, sx, w0.x), qplane(ly, k, sy, w0.y),
+                          qplane(hy, k, sy, w0.y), qplane(lz, k, sz, w0.z), qplane(hz, k, sz, w0.z), rp, tfar);
+    float t0 = c0 == ~0 ? INFINITY : t[0], t1 = c1 == ~0 ? INFINITY : t[1], t2 = c2 == ~0 ? INFINITY : t[2],
+          t3 = c3 == ~0 ? INFINITY : t[3];
+    order2(t0, c0, t1, c1);
+    order2(t2, c2, t3, c3);
+    order2(t0, c0, t2, c2);
+    order2(t1, c1, t3, c3);
+    order2(t1, c1, t2, c2);
+    if (t3 != INFINITY) stack[sp++] = c3;
+    if (t2 != INFINITY) stack[sp++] = c2;
+    if (t1 != INFINITY) stack[sp++] = c1;
+    if (t0 != INFINITY) return c0;
+    return sp > 0 ? stack[--sp] : kTraversalDone;
+}
+
+// One node visit in the scene's node format (warp-uniform branch).
+__device__ __forceinline__ int32_t visit_node(const DevScene& S, int32_t node, const RayPre& rp, float tfar,
+                                              int32_t* stack, int& sp) {
+    return S.qbvh ? visit_quantized(S, node, rp, tfar, stack, sp) : visit_wide(S, node, rp, tfar, stack, sp);
+}
+
 // Stack-based traversal of the four-wide BVH (nearest child first, the other
 // hit children pushed farthest first). ANY: stop at the first hit in (tmin,
 // tmax). Otherwise the result is the lexicographic minimum (t, scene index)
@@ -142,7 +194,7 @@ __device__ __forceinline__ TraceResult traverse(const DevScene& S, v3 o, v3 d, f
     while (true) {
         while (node >= 0) {
             if (COUNT) ++n_nodes;
-            node = visit_wide(S, node, rp, r.t, stack, sp);
+            node = visit_node(S, node, rp, r.t, stack, sp);
         }
         if (node == kTraversalDone) return r;
         // Leaf.
@@ -193,7 +245,7 @@ __device__ __forceinline__ TraceResult traverse_fast(const DevScene& S, v3 o, v3
     int32_t node = 0, leaf = 0;
     while (true) {
         while (node >= 0) {
-            node = visit_wide(S, node, rp, r.t, stack, sp);
+            node = visit_node(S, node, rp, r.t, stack, sp);
             if (node < 0 && node != kTraversalDone && leaf == 0) {
                 leaf = node;
                 node = sp > 0 ? stack[--sp] : kTraversalDone;
@@ -285,7 +337,7 @@ __device__ __forceinline__ void traverse_queue(const DevScene& S, uint32_t n, ui
         if (!have) continue;
         // One round of traverse_fast.
         while (node >= 0) {
-            node = visit_wide(S, node, rp, r.t, stack, sp);
+            node = visit_node(S, node, rp, r.t, stack, sp);
             if (node < 0 && node != kTraversalDone && leaf == 0) {
                 leaf = node;
                 node = sp > 0 ? stack[--sp] : kTraversalDone;

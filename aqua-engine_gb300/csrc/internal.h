@@ -176,6 +176,9 @@ enum { kStatExt = 0, kStatShadow, kStatPaths, kStatNodes, kStatTris, kStatShNode
 struct aqua_scene {
     aq::HostScene host;
     aq::FlatBvh bvh;
+    std::vector<float> qnodes;         // quantized copy of bvh (kBvhQNodeFloats per node)
+    int32_t bvh_format = AQUA_BVH_AUTO;  // requested node format
+    int32_t bvh_format_used = AQUA_BVH_FULL;  // the format of the device image
     void* pinned = nullptr;    // staged device image of the scene
     bool pinned_is_cuda = false;
     size_t bytes = 0;          // bytes of the device image
@@ -208,6 +211,7 @@ struct aqua_ctx {
     aq::DevBuf persist_film;                 // device film of host-film persistent renders
     bool nrc_tc_ready = false;               // tcgen05 inference kernel configured on this device
     bool nrc_tc_bwd_ready = false;           // and the tcgen05 backward kernel
+    bool nrc_tc_wg_ready = false;            // and the tcgen05 weight-gradient kernel
     aq::DevBuf trace_stats;
 };
 
@@ -219,7 +223,10 @@ void dev_free(DevBuf& b);
 
 // Builds the device image of a scene (BVH, triangle words, materials,
 // lights, textures) in pinned memory and copies it to the device.
-void scene_build_device(aqua_ctx* ctx, aqua_scene* s);
+// Quantized nodes are chosen automatically above this many bytes of
+// full-precision nodes (1 MB: past what the SMs' L1 caches hold together).
+constexpr size_t kQuantizeAbove = (size_t)1 << 20;
+void scene_build_device(aqua_ctx* ctx, aqua_scene* s, bool rebuild_bvh = true);
 void scene_upload(aqua_ctx* ctx, aqua_scene* s);
 void scene_release(aqua_scene* s);
 DevCamera dev_camera(const aqua_camera& c);
@@ -259,6 +266,10 @@ size_t nrc_tc_bwd_bytes();
 void nrc_pack_bwd_tc(aqua_ctx* ctx, const float* w, void* img);
 void nrc_backward_tc_dev(aqua_ctx* ctx, const void* img, const float* Y, const float* T, int n, float inv_count,
                          const uint32_t* acts, uint32_t* deltas, uint32_t* d6, double* loss, uint32_t* err);
+// Weight gradients of one training batch on tcgen05: per-chunk partials
+// (chunk-major, kNrcParams each) for the Adam kernel; returns the chunk count.
+int nrc_wgrad_tc_dev(aqua_ctx* ctx, const uint16_t* X, const uint32_t* acts, const uint32_t* deltas,
+                     const uint32_t* d6, int n, float* partial, uint32_t* err);
 // Throws when a tcgen05 launch since the last check gave up waiting (syncs the stream).
 void nrc_check_tc(aqua_ctx* ctx, NrcNet& net);
 

@@ -472,8 +472,13 @@ void nrc_train_step_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, const flo
     else
         k_nrc_backward<<<g, 128, 0, st>>>(net.ty, target, n, 1.0f / (float)(n * kNrcOut), net.fragT, net.acts,
                                           net.deltas, net.d6, net.loss);
-    int chunks = (n + kWgChunk - 1) / kWgChunk;
-    k_nrc_wgrad<<<dim3(chunks, 6), 128, 0, st>>>(Xw, net.acts, net.deltas, net.d6, n, net.partial);
+    int chunks;
+    if (net.forward_tc) {
+        chunks = nrc_wgrad_tc_dev(ctx, X, net.acts, net.deltas, net.d6, n, net.partial, net.tc_err);
+    } else {
+        chunks = (n + kWgChunk - 1) / kWgChunk;
+        k_nrc_wgrad<<<dim3(chunks, 6), 128, 0, st>>>(Xw, net.acts, net.deltas, net.d6, n, net.partial);
+    }
     net.step++;
     float c1 = 1.0f - powf(net.beta1, (float)net.step), c2 = 1.0f - powf(net.beta2, (float)net.step);
     k_nrc_adam<<<(kNrcParams + 255) / 256, 256, 0, st>>>(net.partial, chunks, net.w, net.m, net.v, net.grad, net.lr,

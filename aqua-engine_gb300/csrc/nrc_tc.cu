@@ -599,6 +599,163 @@ void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n
 }
 
 
+// ---------------------------------------------------------------- weight gradients
+// dW_L = D_L^T x H_L over a chunk of kWgTcChunk rows (split-K; the Adam
+// kernel sums the chunk partials in order). Layer L of blockIdx.y: 0..4 ->
+// W1..W5 (H_0 = X, D = delta_{L+1}, 64 columns), 5 -> W6 (H_5, D = dY, 16
+// columns, 3 used). One tcgen05.mma per K = 16 rows: A = D^T (M = 128: the
+// 64 or 16 output features in rows 0.., zero rows above), B = H^T (N = 64
+// input features), both K-major with K = batch rows, accumulating in TMEM
+// (128 lanes x 64 FP32 columns). The 128 threads stage each 128-row slice of
+// D and H transposed into the no-swizzle core-matrix layout (8 batch rows of
+// one feature = one 16-byte core-matrix row; a warp reads 32 consecutive
+// features of a row, 64 contiguous bytes) while the tensor core works on the
+// other of two buffers; thread 0 issues the MMAs and commits each slice to
+// its buffer's mbarrier. All waits are bounded.
+constexpr int kWgTcChunk = 512;                 // rows per CTA (split-K chunk)
+constexpr int kWgTcSlice = 128;                 // rows per staged slice (MMA K = 8 x 16)
+constexpr int kWgTcABytes = 128 * kWgTcSlice * 2;  // A: 128 feature rows x 128 K
+constexpr int kWgTcBBytes = 64 * kWgTcSlice * 2;   // B: 64 feature rows x 128 K
+constexpr int kWgTcSmem = 2 * (kWgTcABytes + kWgTcBBytes) + 1024;
+static_assert(kWgTcChunk % kWgTcSlice == 0, "whole slices per chunk");
+
+__global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict__ X,
+                                                      const uint16_t* __restrict__ acts,
+                                                      const uint16_t* __restrict__ deltas,
+                                                      const uint16_t* __restrict__ d6, int n,
+                                                      float* __restrict__ partial, uint32_t* __restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int L = blockIdx.y, ch = blockIdx.x;
+    const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    uint8_t* sbase = smem_raw + (base - smem_u32(smem_raw));
+    const uint32_t sA[2] = {base, base + (uint32_t)kWgTcABytes};
+    const uint32_t sB[2] = {base + 2u * kWgTcABytes, base + 2u * kWgTcABytes + (uint32_t)kWgTcBBytes};
+    const int dcols = L == 5 ? 16 : 64;
+    const uint16_t* H = L == 0 ? X : acts + (size_t)(L - 1) * (size_t)n * 64;
+    const uint16_t* D = L == 5 ? d6 : deltas + (size_t)L * (size_t)n * 64;
+
+    // A's rows from dcols up stay zero for the whole chunk.
+    for (int i = tid; i < 2 * kWgTcABytes / 16; i += 128) reinterpret_cast<uint4*>(sbase)[i] = make_uint4(0, 0, 0, 0);
+    if (tid < 2) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar[tid])) : "memory");
+    if (tid == 0) asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(64u)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t idesc = tc_idesc(128, 64);
+    const int row_begin = ch * kWgTcChunk;
+    const int slices = kWgTcChunk / kWgTcSlice;
+    uint32_t par[2] = {0, 0};        // parity of each buffer's next completion
+    bool pending[2] = {false, false};  // a commit on the buffer not yet waited for
+    bool ok = true;
+    for (int sl = 0; sl < slices && ok; ++sl) {
+        const int b = sl & 1;
+        if (pending[b]) {  // the MMAs that read this buffer two slices ago
+            bool w = tid == 0 ? mbar_wait(smem_u32(&bar[b]), par[b]) : true;
+            ok = __syncthreads_and(w) != 0;
+            if (!ok) break;  // still pending: the drain below waits for it
+            par[b] ^= 1u;
+            pending[b] = false;
+        }
+        // Stage rows [r0, r0 + 128): feature f of rows 8j..8j+7 -> one 16-byte row.
+        const int r0 = row_begin + sl * kWgTcSlice;
+        uint8_t* a = sbase + (sA[b] - base);
+        uint8_t* bb = sbase + (sB[b] - base);
+        for (int it = tid; it < (64 + dcols) * 16; it += 128) {
+            const bool isA = it >= 64 * 16;
+            const int k = isA ? it - 64 * 16 : it;
+            const int cols = isA ? dcols : 64;
+            const int f = k % cols, j = k / cols;  // consecutive threads: consecutive features
+            const uint16_t* src = (isA ? D : H) + (size_t)(r0 + 8 * j) * (size_t)cols + f;
+            uint32_t v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int ra = r0 + 8 * j + 2 * q;
+                uint32_t lo = ra < n ? (uint32_t)src[(size_t)(2 * q) * cols] : 0u;
+                uint32_t hi = ra + 1 < n ? (uint32_t)src[(size_t)(2 * q + 1) * cols] : 0u;
+                v[q] = lo | (hi << 16);
+            }
+            const int R = isA ? 128 : 64;
+            *reinterpret_cast<uint4*>((isA ? a : bb) + (size_t)j * R * 16 + (size_t)f * 16) =
+                make_uint4(v[0], v[1], v[2], v[3]);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int k = 0; k < kWgTcSlice / 16; ++k)
+                tc_mma(tmem, tc_desc(sA[b] + (uint32_t)k * 2u * (128 * 16), 128 * 16),
+                       tc_desc(sB[b] + (uint32_t)k * 2u * (64 * 16), 64 * 16), idesc, (sl > 0 || k > 0) ? 1u : 0u);
+            tc_commit(smem_u32(&bar[b]));
+        }
+        pending[b] = true;
+    }
+    // Drain: wait (bounded) for every commit still pending, so no MMA runs
+    // when the accumulator is read or the TMEM is freed.
+    for (int b = 0; b < 2; ++b)
+        if (pending[b]) {
+            bool w = tid == 0 ? mbar_wait(smem_u32(&bar[b]), par[b]) : true;
+            ok = (__syncthreads_and(w) != 0) && ok;
+        }
+    tc_fence_after();
+    if (ok) {
+        // Lanes 0..63 hold rows (output features) 0..63; warps 0 and 1 read them.
+        const int orow = warp * 32 + lane;
+        if (warp < 2) {
+            uint32_t r[64];
+            const uint32_t lanes = (uint32_t)(warp * 32) << 16;
+            AQ_TC_LD16(tmem + lanes + 0u, (r + 0));
+            AQ_TC_LD16(tmem + lanes + 16u, (r + 16));
+            AQ_TC_LD16(tmem + lanes + 32u, (r + 32));
+            AQ_TC_LD16(tmem + lanes + 48u, (r + 48));
+            tc_wait_ld();
+            const int mrows = L == 5 ? kNrcOut : 64;
+            if (orow < mrows) {
+                float4* P = reinterpret_cast<float4*>(partial + (size_t)ch * kNrcParams + (size_t)L * 4096 +
+                                                      (size_t)orow * 64);
+#pragma unroll
+                for (int c = 0; c < 16; ++c)
+                    P[c] = make_float4(__uint_as_float(r[4 * c]), __uint_as_float(r[4 * c + 1]),
+                                       __uint_as_float(r[4 * c + 2]), __uint_as_float(r[4 * c + 3]));
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1u);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(64u) : "memory");
+    }
+}
+
+int nrc_wgrad_tc_dev(aqua_ctx* ctx, const uint16_t* X, const uint32_t* acts, const uint32_t* deltas,
+                     const uint32_t* d6, int n, float* partial, uint32_t* err) {
+    if (n <= 0) return 0;
+    if (!ctx->nrc_tc_wg_ready) {
+        AQ_CUDA(cudaFuncSetAttribute(k_nrc_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kWgTcSmem));
+        ctx->nrc_tc_wg_ready = true;
+    }
+    const int chunks = (n + kWgTcChunk - 1) / kWgTcChunk;
+    k_nrc_wgrad_tc<<<dim3(chunks, 6), 128, kWgTcSmem, ctx->stream>>>(
+        X, reinterpret_cast<const uint16_t*>(acts), reinterpret_cast<const uint16_t*>(deltas),
+        reinterpret_cast<const uint16_t*>(d6), n, partial, err);
+    AQ_CUDA(cudaGetLastError());
+    return chunks;
+}
+
 size_t nrc_tc_bwd_bytes() { return (size_t)kTcBwdBytes; }
 
 void nrc_pack_bwd_tc(aqua_ctx* ctx, const float* w, void* img) {

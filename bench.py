@@ -450,6 +450,47 @@ def run_nrc_inference_metric(ctx, bf16_peak: float, peak_src: str, warmup: int =
                          "hbm_gbs": tc["gbs"]}}
 
 
+NRC_TRAIN_FLOP_PER_ROW = 3 * NRC_FLOP_PER_ROW  # forward + activation gradients + weight gradients
+
+
+def run_nrc_training_metric(ctx, peak: float, peak_src: str, warmup: int = 5, steps: int = 20,
+                            batches=(16384, 262144)):
+    """One Adam step of the cache network (tcgen05 forward, backward and
+    weight gradients, Adam) on `batch` device rows of random encoded inputs
+    and targets: rows/s and the tensor roofline of the whole step (useful
+    MLP FLOPs / step time / sustained bf16 peak). 16,384 rows is the cached
+    renderer's batch; the larger batch shows the step when it is not
+    launch-latency bound. Device time from CUDA events (AQUA_NRC_TIMING)."""
+    import torch
+    import aqua
+
+    out = {}
+    for batch in batches:
+        g = torch.Generator(device="cuda").manual_seed(33)
+        raw = torch.rand((batch, 16), generator=g, device="cuda", dtype=torch.float32)
+        x = torch.empty((batch, 64), dtype=torch.int16, device="cuda")
+        tgt = torch.rand((batch, 3), generator=g, device="cuda", dtype=torch.float32)
+        net = aqua.Nrc(ctx, seed=4, bbox_min=[0, 0, 0], bbox_max=[1, 1, 1])
+        net.encode_device(raw.data_ptr(), batch, x.data_ptr())
+        for _ in range(warmup):
+            net.train_step_device(x.data_ptr(), tgt.data_ptr(), batch)
+        ms = [net.train_step_device(x.data_ptr(), tgt.data_ptr(), batch) for _ in range(steps)]
+        net.free()
+        t = statistics.median(ms) * 1e-3
+        tflops = batch * NRC_TRAIN_FLOP_PER_ROW / t / 1e12
+        out[str(batch)] = {"ms_per_step": t * 1e3, "rows_per_s": batch / t, "tflops": tflops,
+                           "frac": tflops / peak}
+        del raw, x, tgt
+    big = out[str(batches[-1])]
+    return {"config": {"workload": "nrc-train-step", "batches": list(batches),
+                       "step": "forward (tcgen05) + backward (tcgen05) + weight gradients (tcgen05) + Adam",
+                       "flop_per_row": NRC_TRAIN_FLOP_PER_ROW},
+            "unit": "Mrows/s", "value": big["rows_per_s"] / 1e6, "steps": steps, "warmup": warmup, "by_batch": out,
+            "roofline": {"bound": "tensor", "achieved": big["tflops"], "peak": peak, "unit": "TFLOP/s",
+                         "frac": big["frac"], "peak_source": peak_src,
+                         "kernel": f"one training step at {batches[-1]} rows (4 launches + weight packing)"}}
+
+
 BATCH_WORKLOAD = {"workload": "batch-64-jobs-4-scenes",
                   "scenes": ["Cornell Lambert (36 tris)", "Cornell GGX (36 tris)",
                              "synthetic interior (1.15M tris, 8 textures)", "random-sphere field (4.0M tris)"],
@@ -639,6 +680,12 @@ def run_gpu(args, world, rank, local, pg):
         nrc_inf = run_nrc_inference_metric(ctx, bf16_peak, "measured (burst)" if "bf16_tflops" in peaks else "fallback",
                                            rows=args.nrc_rows)
 
+    nrc_train = None
+    if rank == 0 and not args.no_nrc:
+        sus = peaks.get("bf16_tflops_sustained", 1700.0)
+        nrc_train = run_nrc_training_metric(ctx, sus, "measured (sustained)" if "bf16_tflops_sustained" in peaks
+                                            else "fallback")
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -667,11 +714,36 @@ def run_gpu(args, world, rank, local, pg):
                 "sphere_field": spheres,
                 "nrc_time_to_relmse": nrc,
                 "nrc_inference": nrc_inf,
+                "nrc_training": nrc_train,
                 "batch": batch,
                 "stage_ms_sampled": {"trace": staged.trace_ms, "shade": staged.shade_ms, "shadow": staged.shadow_ms,
                                      "note": "device ms of every 8th iteration's launches of one render of the "
                                              "step (RENDER_STAGE_TIMING), i.e. about 1/8 of each stage's time"}}
         print(json.dumps(line), flush=True)
+    scene.free()
+    ctx.close()
+
+
+def run_profile_scene(args):
+    """Profiling hook: one render of one procedural scene at its workload's
+    resolution (config 2: the headline workload, 3: the interior, 5: the
+    sphere field) with --spp samples, after 2 warm-up renders, inside the NVTX
+    range "profile_scene". Prints nothing; for ncu captures on a small case."""
+    import torch
+    import aqua
+
+    W = {2: WORKLOAD, 3: INTERIOR_WORKLOAD, 5: SPHERES_WORKLOAD}[args.profile_scene]
+    ctx = aqua.Context(device=0)
+    scene = ctx.procedural(args.profile_scene, seed=0, width=W["width"], height=W["height"])
+    film = torch.zeros(W["width"] * W["height"] * 3, dtype=torch.float32, device="cuda")
+    cfg = ctx.integrator(spp=args.spp or 4, max_depth=W["max_depth"], rr_depth=3, seed=1)
+    for _ in range(2):
+        ctx.render_device(scene, cfg, film.data_ptr())
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("profile_scene")
+    ctx.render_device(scene, cfg, film.data_ptr())
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
     scene.free()
     ctx.close()
 
@@ -702,7 +774,12 @@ def main():
                     help="DRAM bytes per k_trace_ext launch from an ncu capture")
     ap.add_argument("--spp", type=int, default=0,
                     help="samples per pixel of the workload (default 1024; smaller only for profiling captures)")
+    ap.add_argument("--profile-scene", type=int, default=0, choices=[0, 2, 3, 5],
+                    help="profiling hook: render one scene once (with --spp) and exit")
     args = ap.parse_args()
+    if args.profile_scene:
+        run_profile_scene(args)
+        return
     if args.spp > 0 and args.spp != WORKLOAD["spp"]:
         WORKLOAD["spp"] = args.spp
         WORKLOAD["workload"] = f"cornell-ggx-1024x1024-{args.spp}spp-depth8"

@@ -188,8 +188,16 @@ typedef struct aqua_scene_info {
     uint64_t device_bytes;   /* device memory held by the scene             */
     uint64_t upload_bytes;   /* bytes copied host->device by one upload     */
     float env[3];            /* constant radiance seen by escaping rays     */
-    int32_t reserved;
+    int32_t bvh_format;      /* AQUA_BVH_FULL or AQUA_BVH_QUANTIZED: the node
+                                format the device walks                     */
 } aqua_scene_info;
+
+/* BVH node formats. The tree is the same; quantized nodes (64 bytes) hold
+ * the child boxes as 8-bit offsets in a per-node frame, rounded outward
+ * (layout in bvh.h), so walks find the same closest hits while reading half
+ * the bytes per node. AUTO picks quantized nodes when the full-precision
+ * ones exceed 1 MB. */
+enum { AQUA_BVH_AUTO = -1, AQUA_BVH_FULL = 0, AQUA_BVH_QUANTIZED = 1 };
 
 /* Camera, after parsing scenes/cbox.json:516-543 (`Perspective`). */
 typedef struct aqua_camera {
@@ -253,9 +261,10 @@ AQUA_API void aqua_destroy(aqua_ctx* ctx);
  * at most 1024 bytes. */
 AQUA_API const char* aqua_last_error(const aqua_ctx* ctx);
 AQUA_API const char* aqua_status_string(aqua_status s);
-/* ABI version: 100 x major + minor. Major 2: aqua_scene_export_bvh returns
- * the four-wide tree (32 floats per node; major 1 returned a binary tree of
- * 16 floats per node). */
+/* ABI version: 100 x major + minor. Major 3: 64-byte aqua_material with the
+ * Principled lobes, integrator row subsets, BVH node formats. Major 2:
+ * aqua_scene_export_bvh returns the four-wide tree (32 floats per node;
+ * major 1 returned a binary tree of 16 floats per node). */
 #define AQUA_VERSION 300
 AQUA_API int aqua_version(void);
 
@@ -343,6 +352,11 @@ AQUA_API aqua_status aqua_write_image(aqua_ctx* ctx, const char* path, const flo
  * leaf order. */
 AQUA_API aqua_status aqua_scene_export_bvh(aqua_ctx* ctx, const aqua_scene* scene,
                                            float* nodes, int32_t* tri_order);
+/* The quantized copy of the same tree: 16 floats per node (bvh.h). */
+AQUA_API aqua_status aqua_scene_export_bvh_quantized(aqua_ctx* ctx, const aqua_scene* scene, float* nodes);
+/* Selects the node format the device walks (AQUA_BVH_*) and rebuilds the
+ * scene's device image from the tree already built. */
+AQUA_API aqua_status aqua_scene_set_bvh_format(aqua_ctx* ctx, aqua_scene* scene, int32_t format);
 
 /* ---------------------------------------------------------------- integrator */
 /* Parses scenes/integrator.json:1-9. Unknown `type` strings fail with
@@ -402,8 +416,9 @@ typedef struct aqua_nrc aqua_nrc;
 enum { AQUA_NRC_PARAMS = 20672, AQUA_NRC_INPUTS = 64, AQUA_NRC_RAW = 16 };
 enum {
     AQUA_NRC_DEVICE_PTRS = 1u << 0, /* x / raw / out / target are device pointers */
-    AQUA_NRC_TIMING = 1u << 1       /* time the call's device work with CUDA events
-                                       on the context's stream; read it with
+    AQUA_NRC_TIMING = 1u << 1       /* time the call's device work (aqua_nrc_forward,
+                                       aqua_nrc_train_step) with CUDA events on
+                                       the context's stream; read it with
                                        aqua_nrc_last_ms                          */
 };
 

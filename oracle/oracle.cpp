@@ -209,6 +209,33 @@ inline float entry_f(float lox, float hix, float loy, float hiy, float loz, floa
     return tn <= tf ? tn : std::numeric_limits<float>::infinity();
 }
 
+// A quantized node (bvh.h: origin + 8-bit offsets, plane = fmaf(q, 2^(e -
+// 127), origin)) decoded into the 32-float layout the walk reads; empty
+// slots (link ~0) get +inf boxes, which every ray misses, as the device
+// skips them.
+const float* decode_qnode(const orc_scene* s, int32_t i, float* w) {
+    const float* q = s->qnodes + 16 * (size_t)i;
+    uint32_t ex, bytes[6];
+    memcpy(&ex, &q[3], 4);
+    memcpy(bytes, &q[8], 24);
+    int32_t link[4];
+    memcpy(link, &q[4], 16);
+    for (int a = 0; a < 3; ++a) {
+        uint32_t sb = ((ex >> (8 * a)) & 0xffu) << 23;
+        float sc;
+        memcpy(&sc, &sb, 4);
+        for (int k = 0; k < 4; ++k) {
+            const float ql = (float)((bytes[2 * a] >> (8 * k)) & 0xffu);
+            const float qh = (float)((bytes[2 * a + 1] >> (8 * k)) & 0xffu);
+            const bool empty = link[k] == ~0;
+            w[8 * a + k] = empty ? std::numeric_limits<float>::infinity() : std::fmaf(ql, sc, q[a]);
+            w[8 * a + 4 + k] = empty ? std::numeric_limits<float>::infinity() : std::fmaf(qh, sc, q[a]);
+        }
+    }
+    memcpy(&w[24], link, 16);
+    return w;
+}
+
 struct HitF {
     float t, u, v;
     int32_t leaf_idx, id;
@@ -224,10 +251,11 @@ HitF trace_f(const orc_scene* s, V3<float> o, V3<float> d, float tmin, float tma
     auto entry = [&](float lx, float hx, float ly, float hy, float lz, float hz) {
         return entry_f(lx, hx, ly, hy, lz, hz, r, h.t);
     };
+    float qbuf[32];
     while (true) {
         while (node >= 0) {
             h.nodes++;
-            node = visit_wide<float>(node_at(s, node), entry, stack, sp);
+            node = visit_wide<float>(s->qnodes ? decode_qnode(s, node, qbuf) : node_at(s, node), entry, stack, sp);
         }
         if (node == kDone) return h;
         int32_t code = ~node;

@@ -51,6 +51,10 @@ typedef struct orc_scene {
     float env[3];
     const float* nrm;          /* 9 floats per triangle (vertex normals),
                                   scene order, or NULL: flat shading      */
+    const float* qnodes;       /* the quantized copy of the BVH, 16 floats
+                                  per node, when the device walks it (the
+                                  FP32 walk then decodes it as the device
+                                  does), else NULL                        */
 } orc_scene;
 
 /* FP32 traversal of the flattened BVH with the same node order, slab test

@@ -29,7 +29,7 @@ class OrcScene(C.Structure):
                 ("uvs", C.c_void_p), ("tri_mat", C.c_void_p), ("tri_light", C.c_void_p), ("n_tris", C.c_int32),
                 ("mats", C.c_void_p), ("n_mats", C.c_int32), ("lights", C.c_void_p), ("n_lights", C.c_int32),
                 ("tex_rgba", C.c_void_p), ("tex_w", C.c_void_p), ("tex_h", C.c_void_p), ("n_tex", C.c_int32),
-                ("cam", aqua.Camera), ("env", C.c_float * 3), ("nrm", C.c_void_p)]
+                ("cam", aqua.Camera), ("env", C.c_float * 3), ("nrm", C.c_void_p), ("qnodes", C.c_void_p)]
 
 
 _lib = None
@@ -102,6 +102,10 @@ class OracleScene:
         s.cam = scene.camera()
         for i in range(3):
             s.env[i] = info.env[i]
+        if info.bvh_format == aqua.BVH_QUANTIZED:  # walk the nodes the device walks
+            q = scene.bvh_quantized()
+            o.keep.append(q)
+            s.qnodes = _p(q).value
         nrm = scene.normals()
         if nrm is not None:
             o.keep.append(nrm)

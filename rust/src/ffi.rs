@@ -26,6 +26,9 @@ pub const AQUA_ERR_TIMEOUT: aqua_status = 7;
 pub const AQUA_ERR_UNSUPPORTED: aqua_status = 8;
 
 pub const AQUA_VERSION: c_int = 300;  // compare with aqua_version() at start-up
+pub const AQUA_BVH_AUTO: i32 = -1;
+pub const AQUA_BVH_FULL: i32 = 0;
+pub const AQUA_BVH_QUANTIZED: i32 = 1;
 pub const AQUA_DEVICE_HOST_ONLY: i32 = -2;
 pub const AQUA_TRACE_DEVICE_PTRS: u32 = 1 << 0;
 pub const AQUA_TRACE_ANY_HIT: u32 = 1 << 1;
@@ -96,7 +99,7 @@ pub struct aqua_scene_info {
     pub width: i32, pub height: i32,
     pub num_triangles: i32, pub num_materials: i32, pub num_lights: i32, pub num_textures: i32,
     pub num_meshes: i32, pub num_bvh_nodes: i32, pub bvh_depth: i32, pub max_leaf_size: i32,
-    pub device_bytes: u64, pub upload_bytes: u64, pub env: [f32; 3], pub reserved: i32,
+    pub device_bytes: u64, pub upload_bytes: u64, pub env: [f32; 3], pub bvh_format: i32,
 }
 
 #[repr(C)] #[derive(Clone, Copy, Default)]
@@ -167,6 +170,9 @@ extern "C" {
                                      present: *mut i32) -> aqua_status;
     pub fn aqua_scene_export_bvh(ctx: *mut aqua_ctx, scene: *const aqua_scene, nodes: *mut f32,
                                  tri_order: *mut i32) -> aqua_status;
+    pub fn aqua_scene_export_bvh_quantized(ctx: *mut aqua_ctx, scene: *const aqua_scene,
+                                           nodes: *mut f32) -> aqua_status;
+    pub fn aqua_scene_set_bvh_format(ctx: *mut aqua_ctx, scene: *mut aqua_scene, format: i32) -> aqua_status;
 
     // assets and images (host-only contexts too)
     pub fn aqua_decode_jpeg(ctx: *mut aqua_ctx, data: *const u8, n: usize, width: *mut i32,

@@ -157,3 +157,96 @@ def test_stress_trees(host_ctx, tmp_path, kind):
     if kind == "coincident":
         assert set(prim[prim >= 0].tolist()) == {0}
     s.free()
+
+
+def decode_quantized(q):
+    """Planes of the quantized nodes (16 floats each) as the device decodes
+    them: fmaf(byte, 2^(e - 127), origin) in float, i.e. the exact sum in
+    double rounded once to float."""
+    q = np.ascontiguousarray(q, np.float32)
+    words = q.view(np.uint32)
+    origin = q[:, 0:3].astype(np.float64)
+    ex = words[:, 3]
+    lo = np.zeros((q.shape[0], 4, 3), np.float32)
+    hi = np.zeros_like(lo)
+    for a in range(3):
+        e = ((ex >> (8 * a)) & 0xFF).astype(np.int64)
+        assert np.all((e >= 1) & (e <= 254))
+        sc = np.ldexp(1.0, e - 127)
+        for k in range(4):
+            ql = ((words[:, 8 + 2 * a] >> (8 * k)) & 0xFF).astype(np.float64)
+            qh = ((words[:, 9 + 2 * a] >> (8 * k)) & 0xFF).astype(np.float64)
+            lo[:, k, a] = (origin[:, a] + ql * sc).astype(np.float32)
+            hi[:, k, a] = (origin[:, a] + qh * sc).astype(np.float32)
+    return lo, hi, words[:, 4:8].view(np.int32)
+
+
+@pytest.mark.parametrize("config", [1, 2, 3])
+def test_quantized_nodes_contain_the_boxes(host_ctx, config):
+    """Every decoded child box of the quantized copy contains the child's
+    full-precision box, with the same links, and is at most a few of its
+    8-bit steps larger."""
+    s = host_ctx.procedural(config, seed=0, width=32, height=18)
+    nodes, _ = s.bvh()
+    q = s.bvh_quantized()
+    assert q.shape == (nodes.shape[0], 16)
+    lo = np.stack([nodes[:, 0:4], nodes[:, 8:12], nodes[:, 16:20]], axis=-1)
+    hi = np.stack([nodes[:, 4:8], nodes[:, 12:16], nodes[:, 20:24]], axis=-1)
+    link = nodes[:, 24:28].copy().view(np.int32)
+    qlo, qhi, qlink = decode_quantized(q)
+    np.testing.assert_array_equal(qlink, link)
+    real = link != -1
+    assert np.all(qlo[real] <= lo[real]) and np.all(qhi[real] >= hi[real])
+    # Tight: per node and axis the slack is below two steps of the frame.
+    ex = q.view(np.uint32)[:, 3]
+    for a in range(3):
+        step = np.ldexp(1.0, ((ex >> (8 * a)) & 0xFF).astype(np.int64) - 127)[:, None]
+        slack = np.maximum(lo[..., a] - qlo[..., a], qhi[..., a] - hi[..., a])
+        assert np.all(np.where(real, slack <= 2 * step + 1e-30, True))
+    s.free()
+
+
+@pytest.mark.parametrize("kind", ["chain", "cloud", "coincident"])
+def test_quantized_walk_equals_brute_force(host_ctx, tmp_path, kind):
+    """With the quantized nodes selected, the oracle's FP32 walk (which
+    decodes them as the device does) still finds exactly the brute-force
+    closest and any hits; it visits at least as many nodes as the full
+    precision walk."""
+    import pyoracle
+    import aqua
+
+    rng = np.random.default_rng(11)
+    v = soup(kind, rng)
+    verts = v.reshape(-1, 3)
+    idx = np.arange(verts.shape[0]).reshape(-1, 3)
+    write_mesh(tmp_path / "m.mesh", verts.tolist(), idx.tolist(), normals=False)
+    p = tmp_path / "s.json"
+    p.write_text(json.dumps(scene_json([("m.mesh", "w")], {"w": principled()})))
+    s = host_ctx.load_scene(str(p))
+    rays = aimed_rays(v.astype(np.float32), 4000, rng)
+    full = pyoracle.OracleScene.from_aqua(s).trace_bvh_f32(rays)
+    s.set_bvh_format(aqua.BVH_QUANTIZED)
+    assert s.info().bvh_format == aqua.BVH_QUANTIZED
+    o = pyoracle.OracleScene.from_aqua(s)
+    t, u, _, prim, cnt = o.trace_bvh_f32(rays)
+    tb, ub, _, pb = o.trace_brute_f32(rays)
+    np.testing.assert_array_equal(prim, pb)
+    np.testing.assert_array_equal(t.view(np.uint32), tb.view(np.uint32))
+    np.testing.assert_array_equal(u.view(np.uint32), ub.view(np.uint32))
+    occ = o.trace_bvh_f32(rays, any_hit=True)[3]
+    np.testing.assert_array_equal(occ >= 0, pb >= 0)
+    assert cnt[:, 0].sum() >= full[4][:, 0].sum()
+    s.set_bvh_format(aqua.BVH_FULL)
+    assert s.info().bvh_format == aqua.BVH_FULL
+    s.free()
+
+
+def test_automatic_node_format(host_ctx):
+    import aqua
+
+    small = host_ctx.procedural(2, seed=0, width=16, height=16)  # 8 nodes: full precision
+    big = host_ctx.procedural(3, seed=0, width=16, height=16)    # 38 MB of nodes: quantized
+    assert small.info().bvh_format == aqua.BVH_FULL
+    assert big.info().bvh_format == aqua.BVH_QUANTIZED
+    small.free()
+    big.free()

@@ -174,3 +174,36 @@ def test_bad_nrc_arguments(gpu_ctx):
     with pytest.raises(aqua.AquaError) as e:
         aqua.Nrc(gpu_ctx, bbox_min=[0, 0, 0], bbox_max=[1, 0, 1])
     assert e.value.status == aqua.ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("rows", [1, 511, 513, 8229, 70000])
+def test_tcgen05_weight_gradients_equal_mma_sync(gpu_ctx, rows):
+    """The training step's weight gradients on tcgen05 (512-row split-K
+    chunks, TMEM accumulators) against the mma.sync path (128-row chunks) on
+    the same batch: the same bf16 products summed in FP32 in another order,
+    so every layer agrees to accumulation rounding (ragged chunk tails and a
+    single row included). The two nets' forward and backward passes differ
+    only in accumulation order too; rare bf16 rounding flips of the stored
+    activations are the only other difference."""
+    import aqua
+
+    nets = [aqua.Nrc(gpu_ctx, seed=3, learning_rate=1e-2, bbox_min=[-1, -1, -1], bbox_max=[1, 1, 1],
+                     forward_kernel=k) for k in (aqua.NRC_KERNEL_MMA_SYNC, aqua.NRC_KERNEL_TCGEN05)]
+    try:
+        raw = rand_raw(rows, 21)
+        x = nets[0].encode(raw)
+        t = smooth_target(raw)
+        grads = []
+        for n in nets:
+            n.train_step(x, t)
+            grads.append(n.gradients().astype(np.float64))
+    finally:
+        for n in nets:
+            n.free()
+    g0, g1 = grads
+    for l in range(6):
+        sl = slice(l * 4096, l * 4096 + (4096 if l < 5 else 192))
+        scale = np.abs(g0[sl]).max() + 1e-30
+        rel = np.linalg.norm(g1[sl] - g0[sl]) / (np.linalg.norm(g0[sl]) + 1e-30)
+        assert rel < 1e-3 and np.abs(g1[sl] - g0[sl]).max() <= 1e-2 * scale, (l, rel)
+    assert np.any(g1 != 0)

@@ -197,3 +197,33 @@ def test_degenerate_triangle_sets_bit_exact(gpu_ctx, tmp_path, kind):
         assert set(prim[prim >= 0].tolist()) == {0}
     assert_bit_exact(gpu_ctx, s, o, rays, any_hit=True)
     s.free()
+
+
+def test_node_formats_give_identical_hits_and_images(gpu_ctx):
+    """The interior walked through its full-precision and its quantized nodes:
+    every closest and any hit identical bit for bit (decoded boxes contain
+    the true ones, and culling never depends on a box's slack), so images
+    are identical too; the quantized walk counts match the oracle's."""
+    import aqua
+    import pyoracle
+    from conftest import random_rays
+
+    s = gpu_ctx.procedural(3, seed=0, width=64, height=36)
+    assert s.info().bvh_format == aqua.BVH_QUANTIZED
+    rays = random_rays(20000, -9.0, 3.9, seed=9)
+    tq, uq, vq, pq, cq = gpu_ctx.trace(s, rays, count=True)
+    oq = pyoracle.OracleScene.from_aqua(s).trace_bvh_f32(rays)
+    assert np.array_equal(pq, oq[3]) and np.array_equal(tq.view(np.uint32), oq[0].view(np.uint32))
+    assert cq.node_visits == int(oq[4][:, 0].sum()) and cq.tri_tests == int(oq[4][:, 1].sum())
+    cfg = gpu_ctx.integrator(spp=8, max_depth=8, rr_depth=3, seed=6)
+    img_q, _ = gpu_ctx.render(s, cfg)
+    s.set_bvh_format(aqua.BVH_FULL)
+    assert s.info().bvh_format == aqua.BVH_FULL
+    tf, uf, vf, pf, cf = gpu_ctx.trace(s, rays, count=True)
+    assert np.array_equal(pq, pf)
+    assert np.array_equal(tq.view(np.uint32), tf.view(np.uint32))
+    assert np.array_equal(uq.view(np.uint32), uf.view(np.uint32))
+    assert cq.node_visits >= cf.node_visits
+    img_f, _ = gpu_ctx.render(s, cfg)
+    assert np.array_equal(img_q, img_f)
+    s.free()

@@ -175,3 +175,21 @@ def test_render_pixel_list_equals_full_render(cornell_orc):
     assert 0 < pst[0] == 8 * 32 * len(rows) < st[0]
     with pytest.raises(RuntimeError):
         cornell_orc.render_pixels([32 * 32], 1, 1)
+
+
+def test_quantized_walk_equals_brute_force_interior(host_ctx):
+    """The interior picks quantized nodes automatically; the oracle decodes
+    them and its walk still equals brute force, closest and any hit."""
+    import aqua
+
+    s = host_ctx.procedural(3, seed=0, width=32, height=18)
+    assert s.info().bvh_format == aqua.BVH_QUANTIZED
+    o = pyoracle.OracleScene.from_aqua(s)
+    rays = random_rays(400, -9.0, 3.9, seed=5)
+    t, u, v, p, _ = o.trace_bvh_f32(rays)
+    tb, ub, vb, pb = o.trace_brute_f32(rays)
+    assert np.array_equal(p, pb)
+    assert np.array_equal(t.view(np.uint32), tb.view(np.uint32))
+    occ = o.trace_bvh_f32(rays, any_hit=True)[3]
+    assert np.array_equal(occ >= 0, pb >= 0)
+    s.free()
