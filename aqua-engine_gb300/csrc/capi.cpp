@@ -87,9 +87,9 @@ void scene_build_device(aqua_ctx* ctx, aqua_scene* s, bool rebuild_bvh) {
         s->qnodes = quantize_bvh(s->bvh);
     }
     size_t nn = (size_t)s->bvh.num_nodes();
-    // Quantized nodes when asked, or (automatic) when the full-precision
-    // nodes would not stay cache resident: half the bytes per visit for the
-    // memory-bound walks, a few more instructions for the cache-bound ones.
+    // Quantized nodes when asked, or (automatic) for trees whose
+    // full-precision nodes exceed kQuantizeAbove: half the node bytes, a
+    // few more instructions per visit.
     const bool use_q = s->bvh_format == AQUA_BVH_QUANTIZED ||
                        (s->bvh_format == AQUA_BVH_AUTO && nn * sizeof(float) * kBvhNodeFloats > kQuantizeAbove);
     const size_t node_floats = use_q ? kBvhQNodeFloats : kBvhNodeFloats;

@@ -224,8 +224,11 @@ void dev_free(DevBuf& b);
 // Builds the device image of a scene (BVH, triangle words, materials,
 // lights, textures) in pinned memory and copies it to the device.
 // Quantized nodes are chosen automatically above this many bytes of
-// full-precision nodes (1 MB: past what the SMs' L1 caches hold together).
-constexpr size_t kQuantizeAbove = (size_t)1 << 20;
+// full-precision nodes (8 GiB): on GB300 the decode's extra instructions
+// cost more than the halved node bytes save (the 1.15M-triangle interior
+// traced 7% slower, the 4.0M-triangle sphere field 5%), so they pay only
+// where the tree's memory footprint matters.
+constexpr size_t kQuantizeAbove = (size_t)8 << 30;
 void scene_build_device(aqua_ctx* ctx, aqua_scene* s, bool rebuild_bvh = true);
 void scene_upload(aqua_ctx* ctx, aqua_scene* s);
 void scene_release(aqua_scene* s);

@@ -600,7 +600,7 @@ void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n
 
 
 // ---------------------------------------------------------------- weight gradients
-// dW_L = D_L^T x H_L over a chunk of kWgTcChunk rows (split-K; the Adam
+// dW_L = D_L^T x H_L over a chunk of rows (split-K, wgrad_chunk_rows; the Adam
 // kernel sums the chunk partials in order). Layer L of blockIdx.y: 0..4 ->
 // W1..W5 (H_0 = X, D = delta_{L+1}, 64 columns), 5 -> W6 (H_5, D = dY, 16
 // columns, 3 used). One tcgen05.mma per K = 16 rows: A = D^T (M = 128: the
@@ -612,17 +612,25 @@ void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n
 // features of a row, 64 contiguous bytes) while the tensor core works on the
 // other of two buffers; thread 0 issues the MMAs and commits each slice to
 // its buffer's mbarrier. All waits are bounded.
-constexpr int kWgTcChunk = 512;                 // rows per CTA (split-K chunk)
+constexpr int kWgTcChunk = 512;                 // rows per CTA (split-K chunk), at least
+constexpr int kWgTcMaxChunks = 64;              // larger batches get longer chunks
 constexpr int kWgTcSlice = 128;                 // rows per staged slice (MMA K = 8 x 16)
 constexpr int kWgTcABytes = 128 * kWgTcSlice * 2;  // A: 128 feature rows x 128 K
 constexpr int kWgTcBBytes = 64 * kWgTcSlice * 2;   // B: 64 feature rows x 128 K
 constexpr int kWgTcSmem = 2 * (kWgTcABytes + kWgTcBBytes) + 1024;
 static_assert(kWgTcChunk % kWgTcSlice == 0, "whole slices per chunk");
+// Rows per chunk for a batch of n rows: at least kWgTcChunk, and long enough
+// that at most kWgTcMaxChunks partials reach the Adam kernel, which sums
+// every parameter's partials in order (one thread per parameter).
+static int wgrad_chunk_rows(int n) {
+    const int per = (n + kWgTcMaxChunks - 1) / kWgTcMaxChunks;
+    return std::max(kWgTcChunk, (per + kWgTcChunk - 1) / kWgTcChunk * kWgTcChunk);
+}
 
 __global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict__ X,
                                                       const uint16_t* __restrict__ acts,
                                                       const uint16_t* __restrict__ deltas,
-                                                      const uint16_t* __restrict__ d6, int n,
+                                                      const uint16_t* __restrict__ d6, int n, int chunk_rows,
                                                       float* __restrict__ partial, uint32_t* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t bar[2];
@@ -652,8 +660,8 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
     const uint32_t idesc = tc_idesc(128, 64);
-    const int row_begin = ch * kWgTcChunk;
-    const int slices = kWgTcChunk / kWgTcSlice;
+    const int row_begin = ch * chunk_rows;
+    const int slices = min(chunk_rows, n - row_begin + kWgTcSlice - 1) / kWgTcSlice;
     uint32_t par[2] = {0, 0};        // parity of each buffer's next completion
     bool pending[2] = {false, false};  // a commit on the buffer not yet waited for
     bool ok = true;
@@ -748,10 +756,11 @@ int nrc_wgrad_tc_dev(aqua_ctx* ctx, const uint16_t* X, const uint32_t* acts, con
         AQ_CUDA(cudaFuncSetAttribute(k_nrc_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kWgTcSmem));
         ctx->nrc_tc_wg_ready = true;
     }
-    const int chunks = (n + kWgTcChunk - 1) / kWgTcChunk;
+    const int rows = wgrad_chunk_rows(n);
+    const int chunks = (n + rows - 1) / rows;
     k_nrc_wgrad_tc<<<dim3(chunks, 6), 128, kWgTcSmem, ctx->stream>>>(
         X, reinterpret_cast<const uint16_t*>(acts), reinterpret_cast<const uint16_t*>(deltas),
-        reinterpret_cast<const uint16_t*>(d6), n, partial, err);
+        reinterpret_cast<const uint16_t*>(d6), n, rows, partial, err);
     AQ_CUDA(cudaGetLastError());
     return chunks;
 }

@@ -194,9 +194,10 @@ typedef struct aqua_scene_info {
 
 /* BVH node formats. The tree is the same; quantized nodes (64 bytes) hold
  * the child boxes as 8-bit offsets in a per-node frame, rounded outward
- * (layout in bvh.h), so walks find the same closest hits while reading half
- * the bytes per node. AUTO picks quantized nodes when the full-precision
- * ones exceed 1 MB. */
+ * (layout in bvh.h), so walks find the same closest hits from half the node
+ * bytes, at the cost of a few instructions per visit (on GB300 the
+ * full-precision walk is faster for trees of millions of triangles). AUTO
+ * picks quantized nodes only when the full-precision ones exceed 8 GiB. */
 enum { AQUA_BVH_AUTO = -1, AQUA_BVH_FULL = 0, AQUA_BVH_QUANTIZED = 1 };
 
 /* Camera, after parsing scenes/cbox.json:516-543 (`Perspective`). */

@@ -242,11 +242,17 @@ def test_quantized_walk_equals_brute_force(host_ctx, tmp_path, kind):
 
 
 def test_automatic_node_format(host_ctx):
+    """AUTO keeps full-precision nodes below 8 GiB of them (the interior's
+    38 MB included); QUANTIZED and FULL switch the same tree's format."""
     import aqua
 
-    small = host_ctx.procedural(2, seed=0, width=16, height=16)  # 8 nodes: full precision
-    big = host_ctx.procedural(3, seed=0, width=16, height=16)    # 38 MB of nodes: quantized
-    assert small.info().bvh_format == aqua.BVH_FULL
-    assert big.info().bvh_format == aqua.BVH_QUANTIZED
-    small.free()
+    big = host_ctx.procedural(3, seed=0, width=16, height=16)
+    assert big.info().bvh_format == aqua.BVH_FULL
+    n = big.info().num_bvh_nodes
+    big.set_bvh_format(aqua.BVH_QUANTIZED)
+    assert big.info().bvh_format == aqua.BVH_QUANTIZED and big.info().num_bvh_nodes == n
+    big.set_bvh_format(aqua.BVH_AUTO)
+    assert big.info().bvh_format == aqua.BVH_FULL
+    with pytest.raises(aqua.AquaError):
+        big.set_bvh_format(7)
     big.free()

@@ -209,6 +209,7 @@ def test_node_formats_give_identical_hits_and_images(gpu_ctx):
     from conftest import random_rays
 
     s = gpu_ctx.procedural(3, seed=0, width=64, height=36)
+    s.set_bvh_format(aqua.BVH_QUANTIZED)
     assert s.info().bvh_format == aqua.BVH_QUANTIZED
     rays = random_rays(20000, -9.0, 3.9, seed=9)
     tq, uq, vq, pq, cq = gpu_ctx.trace(s, rays, count=True)

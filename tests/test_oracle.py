@@ -178,11 +178,12 @@ def test_render_pixel_list_equals_full_render(cornell_orc):
 
 
 def test_quantized_walk_equals_brute_force_interior(host_ctx):
-    """The interior picks quantized nodes automatically; the oracle decodes
-    them and its walk still equals brute force, closest and any hit."""
+    """The interior with quantized nodes: the oracle decodes them and its
+    walk still equals brute force, closest and any hit."""
     import aqua
 
     s = host_ctx.procedural(3, seed=0, width=32, height=18)
+    s.set_bvh_format(aqua.BVH_QUANTIZED)
     assert s.info().bvh_format == aqua.BVH_QUANTIZED
     o = pyoracle.OracleScene.from_aqua(s)
     rays = random_rays(400, -9.0, 3.9, seed=5)
