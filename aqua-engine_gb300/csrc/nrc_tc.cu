@@ -639,8 +639,10 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict
     const int L = blockIdx.y, ch = blockIdx.x;
     const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
     uint8_t* sbase = smem_raw + (base - smem_u32(smem_raw));
-    const uint32_t sA[2] = {base, base + (uint32_t)kWgTcABytes};
-    const uint32_t sB[2] = {base + 2u * kWgTcABytes, base + 2u * kWgTcABytes + (uint32_t)kWgTcBBytes};
+    // Buffer b: A at base + b * kWgTcABytes, B after both A buffers (no
+    // arrays indexed by b, so nothing lands in local memory).
+    auto sA = [&](int b) { return base + (uint32_t)b * (uint32_t)kWgTcABytes; };
+    auto sB = [&](int b) { return base + 2u * kWgTcABytes + (uint32_t)b * (uint32_t)kWgTcBBytes; };
     const int dcols = L == 5 ? 16 : 64;
     const uint16_t* H = L == 0 ? X : acts + (size_t)(L - 1) * (size_t)n * 64;
     const uint16_t* D = L == 5 ? d6 : deltas + (size_t)L * (size_t)n * 64;
@@ -662,22 +664,23 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict
     const uint32_t idesc = tc_idesc(128, 64);
     const int row_begin = ch * chunk_rows;
     const int slices = min(chunk_rows, n - row_begin + kWgTcSlice - 1) / kWgTcSlice;
-    uint32_t par[2] = {0, 0};        // parity of each buffer's next completion
-    bool pending[2] = {false, false};  // a commit on the buffer not yet waited for
+    // Per buffer: the parity of its next completion and whether a commit
+    // on it has not been waited for (bit b of par / pending).
+    uint32_t par = 0, pending = 0;
     bool ok = true;
     for (int sl = 0; sl < slices && ok; ++sl) {
         const int b = sl & 1;
-        if (pending[b]) {  // the MMAs that read this buffer two slices ago
-            bool w = tid == 0 ? mbar_wait(smem_u32(&bar[b]), par[b]) : true;
+        if (pending & (1u << b)) {  // the MMAs that read this buffer two slices ago
+            bool w = tid == 0 ? mbar_wait(smem_u32(&bar[b]), (par >> b) & 1u) : true;
             ok = __syncthreads_and(w) != 0;
             if (!ok) break;  // still pending: the drain below waits for it
-            par[b] ^= 1u;
-            pending[b] = false;
+            par ^= 1u << b;
+            pending &= ~(1u << b);
         }
         // Stage rows [r0, r0 + 128): feature f of rows 8j..8j+7 -> one 16-byte row.
         const int r0 = row_begin + sl * kWgTcSlice;
-        uint8_t* a = sbase + (sA[b] - base);
-        uint8_t* bb = sbase + (sB[b] - base);
+        uint8_t* a = sbase + (sA(b) - base);
+        uint8_t* bb = sbase + (sB(b) - base);
         for (int it = tid; it < (64 + dcols) * 16; it += 128) {
             const bool isA = it >= 64 * 16;
             const int k = isA ? it - 64 * 16 : it;
@@ -703,17 +706,18 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict
             tc_fence_after();
 #pragma unroll
             for (int k = 0; k < kWgTcSlice / 16; ++k)
-                tc_mma(tmem, tc_desc(sA[b] + (uint32_t)k * 2u * (128 * 16), 128 * 16),
-                       tc_desc(sB[b] + (uint32_t)k * 2u * (64 * 16), 64 * 16), idesc, (sl > 0 || k > 0) ? 1u : 0u);
+                tc_mma(tmem, tc_desc(sA(b) + (uint32_t)k * 2u * (128 * 16), 128 * 16),
+                       tc_desc(sB(b) + (uint32_t)k * 2u * (64 * 16), 64 * 16), idesc, (sl > 0 || k > 0) ? 1u : 0u);
             tc_commit(smem_u32(&bar[b]));
         }
-        pending[b] = true;
+        pending |= 1u << b;
     }
     // Drain: wait (bounded) for every commit still pending, so no MMA runs
     // when the accumulator is read or the TMEM is freed.
+#pragma unroll
     for (int b = 0; b < 2; ++b)
-        if (pending[b]) {
-            bool w = tid == 0 ? mbar_wait(smem_u32(&bar[b]), par[b]) : true;
+        if (pending & (1u << b)) {
+            bool w = tid == 0 ? mbar_wait(smem_u32(&bar[b]), (par >> b) & 1u) : true;
             ok = (__syncthreads_and(w) != 0) && ok;
         }
     tc_fence_after();

@@ -776,9 +776,19 @@ def main():
                     help="samples per pixel of the workload (default 1024; smaller only for profiling captures)")
     ap.add_argument("--profile-scene", type=int, default=0, choices=[0, 2, 3, 5],
                     help="profiling hook: render one scene once (with --spp) and exit")
+    ap.add_argument("--profile-train", type=int, default=0,
+                    help="profiling hook: time cache training steps on this many rows and exit")
     args = ap.parse_args()
     if args.profile_scene:
         run_profile_scene(args)
+        return
+    if args.profile_train:
+        import aqua
+
+        ctx = aqua.Context(device=0)
+        r = run_nrc_training_metric(ctx, 1700.0, "fallback", warmup=2, steps=3, batches=(args.profile_train,))
+        log(json.dumps(r["by_batch"]))
+        ctx.close()
         return
     if args.spp > 0 and args.spp != WORKLOAD["spp"]:
         WORKLOAD["spp"] = args.spp
