@@ -606,18 +606,21 @@ void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n
 // columns, 3 used). One tcgen05.mma per K = 16 rows: A = D^T (M = 128: the
 // 64 or 16 output features in rows 0.., zero rows above), B = H^T (N = 64
 // input features), both K-major with K = batch rows, accumulating in TMEM
-// (128 lanes x 64 FP32 columns). The 128 threads stage each 128-row slice of
-// D and H transposed into the no-swizzle core-matrix layout (8 batch rows of
-// one feature = one 16-byte core-matrix row; a warp reads 32 consecutive
-// features of a row, 64 contiguous bytes) while the tensor core works on the
-// other of two buffers; thread 0 issues the MMAs and commits each slice to
+// (128 lanes x 64 FP32 columns). The 128 threads read each 128-row slice of
+// D and H with coalesced 16-byte loads (issued one slice ahead, into
+// registers), store it row-major to shared memory and transpose it there into
+// the no-swizzle core-matrix layout (8 batch rows of one feature = one
+// 16-byte core-matrix row) while the tensor core works on the other of two
+// buffers; thread 0 issues the MMAs and commits each slice to
 // its buffer's mbarrier. All waits are bounded.
 constexpr int kWgTcChunk = 512;                 // rows per CTA (split-K chunk), at least
 constexpr int kWgTcMaxChunks = 64;              // larger batches get longer chunks
 constexpr int kWgTcSlice = 128;                 // rows per staged slice (MMA K = 8 x 16)
 constexpr int kWgTcABytes = 128 * kWgTcSlice * 2;  // A: 128 feature rows x 128 K
 constexpr int kWgTcBBytes = 64 * kWgTcSlice * 2;   // B: 64 feature rows x 128 K
-constexpr int kWgTcSmem = 2 * (kWgTcABytes + kWgTcBBytes) + 1024;
+constexpr int kWgTcRawStride = 144;  // bytes per raw staged row: 128 + 16 (16-byte aligned; 8 rows start on 8 banks)
+constexpr int kWgTcRawBytes = kWgTcSlice * kWgTcRawStride;
+constexpr int kWgTcSmem = 2 * (kWgTcABytes + kWgTcBBytes) + 2 * kWgTcRawBytes + 1024;
 static_assert(kWgTcChunk % kWgTcSlice == 0, "whole slices per chunk");
 // Rows per chunk for a batch of n rows: at least kWgTcChunk, and long enough
 // that at most kWgTcMaxChunks partials reach the Adam kernel, which sums
@@ -664,6 +667,34 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict
     const uint32_t idesc = tc_idesc(128, 64);
     const int row_begin = ch * chunk_rows;
     const int slices = min(chunk_rows, n - row_begin + kWgTcSlice - 1) / kWgTcSlice;
+    // Raw row-major staging of one slice: H rows (128 B) and D rows (128 or
+    // 32 B), read with coalesced 16-byte loads into registers (zero past n).
+    uint8_t* rawH = sbase + 2 * kWgTcABytes + 2 * kWgTcBBytes;
+    uint8_t* rawD = rawH + kWgTcRawBytes;
+    const int dq = dcols / 8;  // 16-byte words per D row
+    uint4 rh[8], rd[8];
+    auto load_rows = [&](int r0) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int idx = tid + 128 * q, row = r0 + (idx >> 3);
+            rh[q] = row < n ? reinterpret_cast<const uint4*>(H + (size_t)row * 64)[idx & 7] : make_uint4(0, 0, 0, 0);
+            const int row_d = r0 + idx / dq;
+            rd[q] = (idx < kWgTcSlice * dq && row_d < n)
+                        ? reinterpret_cast<const uint4*>(D + (size_t)row_d * dcols)[idx % dq]
+                        : make_uint4(0, 0, 0, 0);
+        }
+    };
+    auto store_raw = [&]() {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int idx = tid + 128 * q;
+            *reinterpret_cast<uint4*>(rawH + (size_t)(idx >> 3) * kWgTcRawStride + (size_t)(idx & 7) * 16) = rh[q];
+            if (idx < kWgTcSlice * dq)
+                *reinterpret_cast<uint4*>(rawD + (size_t)(idx / dq) * kWgTcRawStride + (size_t)(idx % dq) * 16) =
+                    rd[q];
+        }
+    };
+    load_rows(row_begin);
     // Per buffer: the parity of its next completion and whether a commit
     // on it has not been waited for (bit b of par / pending).
     uint32_t par = 0, pending = 0;
@@ -677,8 +708,13 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict
             par ^= 1u << b;
             pending &= ~(1u << b);
         }
-        // Stage rows [r0, r0 + 128): feature f of rows 8j..8j+7 -> one 16-byte row.
-        const int r0 = row_begin + sl * kWgTcSlice;
+        // The slice's rows, prefetched into registers during the previous
+        // slice, go to the raw buffers as they are (row-major); the next
+        // slice's rows are requested before this one is transposed.
+        store_raw();
+        if (sl + 1 < slices) load_rows(row_begin + (sl + 1) * kWgTcSlice);
+        __syncthreads();
+        // Transpose: feature f of rows 8j..8j+7 -> one 16-byte core-matrix row.
         uint8_t* a = sbase + (sA(b) - base);
         uint8_t* bb = sbase + (sB(b) - base);
         for (int it = tid; it < (64 + dcols) * 16; it += 128) {
@@ -686,15 +722,13 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict
             const int k = isA ? it - 64 * 16 : it;
             const int cols = isA ? dcols : 64;
             const int f = k % cols, j = k / cols;  // consecutive threads: consecutive features
-            const uint16_t* src = (isA ? D : H) + (size_t)(r0 + 8 * j) * (size_t)cols + f;
+            const uint8_t* src = (isA ? rawD : rawH) + (size_t)(8 * j) * kWgTcRawStride + (size_t)f * 2;
             uint32_t v[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int ra = r0 + 8 * j + 2 * q;
-                uint32_t lo = ra < n ? (uint32_t)src[(size_t)(2 * q) * cols] : 0u;
-                uint32_t hi = ra + 1 < n ? (uint32_t)src[(size_t)(2 * q + 1) * cols] : 0u;
-                v[q] = lo | (hi << 16);
-            }
+            for (int q = 0; q < 4; ++q)
+                v[q] = (uint32_t)*reinterpret_cast<const uint16_t*>(src + (size_t)(2 * q) * kWgTcRawStride) |
+                       ((uint32_t)*reinterpret_cast<const uint16_t*>(src + (size_t)(2 * q + 1) * kWgTcRawStride)
+                        << 16);
             const int R = isA ? 128 : 64;
             *reinterpret_cast<uint4*>((isA ? a : bb) + (size_t)j * R * 16 + (size_t)f * 16) =
                 make_uint4(v[0], v[1], v[2], v[3]);

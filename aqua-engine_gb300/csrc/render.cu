@@ -155,6 +155,29 @@ __device__ __forceinline__ bool start_path(const DevScene& S, const WaveParams& 
     return true;
 }
 
+// Block-aggregated append: every thread of the block calls it together;
+// threads with pred set get consecutive entries of *ctr, with one atomic per
+// block instead of one per warp. s_warp: (warps + 1) shared words.
+__device__ __forceinline__ uint32_t block_append(uint32_t* ctr, bool pred, uint32_t* s_warp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned m = __ballot_sync(0xffffffffu, pred);
+    if (lane == 0) s_warp[warp] = (uint32_t)__popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int w = 0; w < nw; ++w) {
+            const uint32_t c = s_warp[w];
+            s_warp[w] = acc;
+            acc += c;
+        }
+        s_warp[nw] = acc ? atomicAdd(ctr, acc) : 0u;
+    }
+    __syncthreads();
+    const uint32_t k = s_warp[nw] + s_warp[warp] + (uint32_t)__popc(m & ((1u << lane) - 1u));
+    __syncthreads();  // s_warp is reused by the next call
+    return k;
+}
+
 __device__ __forceinline__ void film_add(float4* film, uint32_t pixel, v3 c) {
     float4 f = film[pixel];
     f.x += c.x; f.y += c.y; f.z += c.z;
@@ -294,8 +317,13 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
     }
     uint32_t* out_cnt = &W.counters[cnt_out];
     unsigned long long done_paths = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t s;
+    __shared__ uint32_t s_warp[5];
+    // The whole block iterates together (the out-queue append is per block).
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+        const uint32_t i = i0 + threadIdx.x;
+        uint32_t s = 0;
+        bool cont = false;
+        if (i < n) {
         // With sorted queues the bucket is the material, so its parameters
         // load alongside the path state instead of after the triangle.
         float4 mat_a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), mat_b = mat_a;
@@ -326,7 +354,6 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
         v3 thr = f3(tpv);
         float pdf_b = tpv.w;
         int32_t tri = __float_as_int(h.w);
-        bool cont = false;
         if (tri < 0) {
             v3 e = mk(S.env[0], S.env[1], S.env[2]);
             if (e.x > 0.0f || e.y > 0.0f || e.z > 0.0f) film_add(W.film, pixel, thr * e);
@@ -509,7 +536,8 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
             ++done_paths;
             cont = start_path<NRC>(S, P, W, s, j + 1);
         }
-        uint32_t k = warp_append(out_cnt, cont);
+        }
+        const uint32_t k = block_append(out_cnt, cont, s_warp);
         if (cont) W.q_out[k] = s;
     }
     for (int o = 16; o > 0; o >>= 1) done_paths += __shfl_down_sync(0xffffffffu, done_paths, o);

@@ -333,6 +333,9 @@ SPHERES_WORKLOAD = {"workload": "sphere-field-1024x1024-64spp-depth8", "width": 
 TRACE_TRAFFIC = {
     "interior": {"bytes": 564.4e6, "rays": 2073600,
                  "source": "profiles/trace_interior-1920x1080-256spp.md (497.3 MB read + 67.1 MB written)"},
+    "spheres": {"bytes": 180.36e6, "rays": 1048576,
+                "source": "profiles/trace_sphere-field-1024x1024.md (172.6 MB read + 7.7 MB written, the render's "
+                          "third launch: full queue of camera and first-bounce rays)"},
 }
 
 
