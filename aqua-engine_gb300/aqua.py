@@ -82,6 +82,7 @@ class Tuning(C.Structure):
 
 KERNEL_WAVEFRONT, KERNEL_PERSISTENT = 0, 1
 BVH_AUTO, BVH_FULL, BVH_QUANTIZED = -1, 0, 1
+NRC_QUERY_SPREAD = -1
 
 
 class Stats(C.Structure):

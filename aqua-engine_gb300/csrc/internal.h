@@ -136,6 +136,7 @@ struct NrcWorkspace {
     float4* rec = nullptr;       // training-vertex records (6 words each)
     float4* ltrain = nullptr;    // radiance per training path
     float4* lsnap = nullptr;     // per training path and bounce: radiance before it
+    float2* spread = nullptr;    // per path slot: path-spread sum and a0
     size_t snaps = 0;            // bounces per training path (capacity)
     float* t_raw = nullptr;      // permuted training features
     uint16_t* t_x = nullptr;     // encoded training inputs

@@ -606,13 +606,14 @@ void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n
 // columns, 3 used). One tcgen05.mma per K = 16 rows: A = D^T (M = 128: the
 // 64 or 16 output features in rows 0.., zero rows above), B = H^T (N = 64
 // input features), both K-major with K = batch rows, accumulating in TMEM
-// (128 lanes x 64 FP32 columns). The 128 threads read each 128-row slice of
+// (128 lanes x 64 FP32 columns). The 256 threads read each 128-row slice of
 // D and H with coalesced 16-byte loads (issued one slice ahead, into
 // registers), store it row-major to shared memory and transpose it there into
 // the no-swizzle core-matrix layout (8 batch rows of one feature = one
-// 16-byte core-matrix row) while the tensor core works on the other of two
-// buffers; thread 0 issues the MMAs and commits each slice to
-// its buffer's mbarrier. All waits are bounded.
+// 16-byte core-matrix row); thread 0 issues the slice's MMAs and commits them
+// to an mbarrier, which the next slice's transpose waits for. The 84 KB of
+// shared memory let two CTAs share an SM. All waits are bounded.
+constexpr int kWgTcThreads = 256;
 constexpr int kWgTcChunk = 512;                 // rows per CTA (split-K chunk), at least
 constexpr int kWgTcMaxChunks = 64;              // larger batches get longer chunks
 constexpr int kWgTcSlice = 128;                 // rows per staged slice (MMA K = 8 x 16)
@@ -620,8 +621,10 @@ constexpr int kWgTcABytes = 128 * kWgTcSlice * 2;  // A: 128 feature rows x 128 
 constexpr int kWgTcBBytes = 64 * kWgTcSlice * 2;   // B: 64 feature rows x 128 K
 constexpr int kWgTcRawStride = 144;  // bytes per raw staged row: 128 + 16 (16-byte aligned; 8 rows start on 8 banks)
 constexpr int kWgTcRawBytes = kWgTcSlice * kWgTcRawStride;
-constexpr int kWgTcSmem = 2 * (kWgTcABytes + kWgTcBBytes) + 2 * kWgTcRawBytes + 1024;
+constexpr int kWgTcSmem = kWgTcABytes + kWgTcBBytes + 2 * kWgTcRawBytes + 1024;
+constexpr int kWgTcLoads = kWgTcSlice * 8 / kWgTcThreads;  // 16-byte loads per thread per matrix and slice
 static_assert(kWgTcChunk % kWgTcSlice == 0, "whole slices per chunk");
+static_assert(2 * kWgTcSmem <= 227 * 1024, "two CTAs per SM");
 // Rows per chunk for a batch of n rows: at least kWgTcChunk, and long enough
 // that at most kWgTcMaxChunks partials reach the Adam kernel, which sums
 // every parameter's partials in order (one thread per parameter).
@@ -630,30 +633,34 @@ static int wgrad_chunk_rows(int n) {
     return std::max(kWgTcChunk, (per + kWgTcChunk - 1) / kWgTcChunk * kWgTcChunk);
 }
 
-__global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict__ X,
-                                                      const uint16_t* __restrict__ acts,
-                                                      const uint16_t* __restrict__ deltas,
-                                                      const uint16_t* __restrict__ d6, int n, int chunk_rows,
-                                                      float* __restrict__ partial, uint32_t* __restrict__ err) {
+__global__ void __launch_bounds__(kWgTcThreads, 2) k_nrc_wgrad_tc(const uint16_t* __restrict__ X,
+                                                                  const uint16_t* __restrict__ acts,
+                                                                  const uint16_t* __restrict__ deltas,
+                                                                  const uint16_t* __restrict__ d6, int n,
+                                                                  int chunk_rows, float* __restrict__ partial,
+                                                                  uint32_t* __restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int L = blockIdx.y, ch = blockIdx.x;
     const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
     uint8_t* sbase = smem_raw + (base - smem_u32(smem_raw));
-    // Buffer b: A at base + b * kWgTcABytes, B after both A buffers (no
-    // arrays indexed by b, so nothing lands in local memory).
-    auto sA = [&](int b) { return base + (uint32_t)b * (uint32_t)kWgTcABytes; };
-    auto sB = [&](int b) { return base + 2u * kWgTcABytes + (uint32_t)b * (uint32_t)kWgTcBBytes; };
+    const uint32_t sA = base, sB = base + (uint32_t)kWgTcABytes;
+    uint8_t* a = sbase;
+    uint8_t* bb = sbase + kWgTcABytes;
+    uint8_t* rawH = bb + kWgTcBBytes;
+    uint8_t* rawD = rawH + kWgTcRawBytes;
     const int dcols = L == 5 ? 16 : 64;
     const uint16_t* H = L == 0 ? X : acts + (size_t)(L - 1) * (size_t)n * 64;
     const uint16_t* D = L == 5 ? d6 : deltas + (size_t)L * (size_t)n * 64;
 
     // A's rows from dcols up stay zero for the whole chunk.
-    for (int i = tid; i < 2 * kWgTcABytes / 16; i += 128) reinterpret_cast<uint4*>(sbase)[i] = make_uint4(0, 0, 0, 0);
-    if (tid < 2) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar[tid])) : "memory");
-    if (tid == 0) asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    for (int i = tid; i < kWgTcABytes / 16; i += kWgTcThreads) reinterpret_cast<uint4*>(a)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
                      "r"(64u)
@@ -669,14 +676,12 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict
     const int slices = min(chunk_rows, n - row_begin + kWgTcSlice - 1) / kWgTcSlice;
     // Raw row-major staging of one slice: H rows (128 B) and D rows (128 or
     // 32 B), read with coalesced 16-byte loads into registers (zero past n).
-    uint8_t* rawH = sbase + 2 * kWgTcABytes + 2 * kWgTcBBytes;
-    uint8_t* rawD = rawH + kWgTcRawBytes;
     const int dq = dcols / 8;  // 16-byte words per D row
-    uint4 rh[8], rd[8];
+    uint4 rh[kWgTcLoads], rd[kWgTcLoads];
     auto load_rows = [&](int r0) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int idx = tid + 128 * q, row = r0 + (idx >> 3);
+        for (int q = 0; q < kWgTcLoads; ++q) {
+            const int idx = tid + kWgTcThreads * q, row = r0 + (idx >> 3);
             rh[q] = row < n ? reinterpret_cast<const uint4*>(H + (size_t)row * 64)[idx & 7] : make_uint4(0, 0, 0, 0);
             const int row_d = r0 + idx / dq;
             rd[q] = (idx < kWgTcSlice * dq && row_d < n)
@@ -686,8 +691,8 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict
     };
     auto store_raw = [&]() {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int idx = tid + 128 * q;
+        for (int q = 0; q < kWgTcLoads; ++q) {
+            const int idx = tid + kWgTcThreads * q;
             *reinterpret_cast<uint4*>(rawH + (size_t)(idx >> 3) * kWgTcRawStride + (size_t)(idx & 7) * 16) = rh[q];
             if (idx < kWgTcSlice * dq)
                 *reinterpret_cast<uint4*>(rawD + (size_t)(idx / dq) * kWgTcRawStride + (size_t)(idx % dq) * 16) =
@@ -695,29 +700,26 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict
         }
     };
     load_rows(row_begin);
-    // Per buffer: the parity of its next completion and whether a commit
-    // on it has not been waited for (bit b of par / pending).
-    uint32_t par = 0, pending = 0;
+    uint32_t par = 0;      // parity of the mbarrier's next completion
+    bool pending = false;  // the last slice's MMAs not yet waited for
     bool ok = true;
-    for (int sl = 0; sl < slices && ok; ++sl) {
-        const int b = sl & 1;
-        if (pending & (1u << b)) {  // the MMAs that read this buffer two slices ago
-            bool w = tid == 0 ? mbar_wait(smem_u32(&bar[b]), (par >> b) & 1u) : true;
-            ok = __syncthreads_and(w) != 0;
-            if (!ok) break;  // still pending: the drain below waits for it
-            par ^= 1u << b;
-            pending &= ~(1u << b);
-        }
-        // The slice's rows, prefetched into registers during the previous
-        // slice, go to the raw buffers as they are (row-major); the next
-        // slice's rows are requested before this one is transposed.
+    for (int sl = 0; sl < slices; ++sl) {
+        // The slice's rows (prefetched) go to the raw buffers as they are;
+        // the next slice's rows are requested before this one is transposed.
         store_raw();
         if (sl + 1 < slices) load_rows(row_begin + (sl + 1) * kWgTcSlice);
-        __syncthreads();
+        // The previous slice's MMAs must have read A and B before the
+        // transpose overwrites them.
+        bool w = true;
+        if (pending && tid == 0) w = mbar_wait(smem_u32(&bar), par);
+        ok = __syncthreads_and(w) != 0;  // also: the raw buffers are complete
+        if (!ok) break;  // still pending: the drain below waits for it
+        if (pending) {
+            par ^= 1u;
+            pending = false;
+        }
         // Transpose: feature f of rows 8j..8j+7 -> one 16-byte core-matrix row.
-        uint8_t* a = sbase + (sA(b) - base);
-        uint8_t* bb = sbase + (sB(b) - base);
-        for (int it = tid; it < (64 + dcols) * 16; it += 128) {
+        for (int it = tid; it < (64 + dcols) * 16; it += kWgTcThreads) {
             const bool isA = it >= 64 * 16;
             const int k = isA ? it - 64 * 16 : it;
             const int cols = isA ? dcols : 64;
@@ -735,25 +737,23 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad_tc(const uint16_t* __restrict
         }
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
+        __syncthreads();  // the transpose is complete (and the raw buffers free)
         if (tid == 0) {
             tc_fence_after();
 #pragma unroll
             for (int k = 0; k < kWgTcSlice / 16; ++k)
-                tc_mma(tmem, tc_desc(sA(b) + (uint32_t)k * 2u * (128 * 16), 128 * 16),
-                       tc_desc(sB(b) + (uint32_t)k * 2u * (64 * 16), 64 * 16), idesc, (sl > 0 || k > 0) ? 1u : 0u);
-            tc_commit(smem_u32(&bar[b]));
+                tc_mma(tmem, tc_desc(sA + (uint32_t)k * 2u * (128 * 16), 128 * 16),
+                       tc_desc(sB + (uint32_t)k * 2u * (64 * 16), 64 * 16), idesc, (sl > 0 || k > 0) ? 1u : 0u);
+            tc_commit(smem_u32(&bar));
         }
-        pending |= 1u << b;
+        pending = true;
     }
-    // Drain: wait (bounded) for every commit still pending, so no MMA runs
-    // when the accumulator is read or the TMEM is freed.
-#pragma unroll
-    for (int b = 0; b < 2; ++b)
-        if (pending & (1u << b)) {
-            bool w = tid == 0 ? mbar_wait(smem_u32(&bar[b]), (par >> b) & 1u) : true;
-            ok = (__syncthreads_and(w) != 0) && ok;
-        }
+    // Drain: wait (bounded) for the commit still pending, so no MMA runs when
+    // the accumulator is read or the TMEM is freed.
+    if (pending) {
+        bool w = tid == 0 ? mbar_wait(smem_u32(&bar), par) : true;
+        ok = (__syncthreads_and(w) != 0) && ok;
+    }
     tc_fence_after();
     if (ok) {
         // Lanes 0..63 hold rows (output features) 0..63; warps 0 and 1 read them.
@@ -796,7 +796,7 @@ int nrc_wgrad_tc_dev(aqua_ctx* ctx, const uint16_t* X, const uint32_t* acts, con
     }
     const int rows = wgrad_chunk_rows(n);
     const int chunks = (n + rows - 1) / rows;
-    k_nrc_wgrad_tc<<<dim3(chunks, 6), 128, kWgTcSmem, ctx->stream>>>(
+    k_nrc_wgrad_tc<<<dim3(chunks, 6), kWgTcThreads, kWgTcSmem, ctx->stream>>>(
         X, reinterpret_cast<const uint16_t*>(acts), reinterpret_cast<const uint16_t*>(deltas),
         reinterpret_cast<const uint16_t*>(d6), n, rows, partial, err);
     AQ_CUDA(cudaGetLastError());

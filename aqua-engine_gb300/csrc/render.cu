@@ -33,7 +33,8 @@ struct WaveParams {
     uint32_t slots, pixels;
     uint32_t nb;  // material buckets incl. the miss bucket (0 = unsorted)
     // Radiance cache (NRC mode only).
-    int32_t query_depth;       // bounce at which non-training paths query the cache
+    int32_t query_depth;       // bounce at which non-training paths query the cache (-1: by path spread)
+    float spread_c;            // path-spread mode: query once spread > spread_c x a0
     uint32_t train_thresh;     // path trains when its 24-bit hash < this
     uint32_t max_train_paths;  // capacity of the per-training-path accumulators
     uint32_t max_records;      // capacity of the training-vertex records
@@ -69,6 +70,7 @@ struct WavePtrs {
     float* q_raw;     // per query: 16 raw vertex features
     float4* rec;      // per training vertex: 6 words (raw 16, throughput 3, radiance-before 3, path id)
     float4* ltrain;   // per training path: radiance gathered so far
+    float2* spread;   // per slot: (sum of sqrt spread terms, a0) of the path (path-spread mode)
     float4* lsnap;    // per training path and bounce k < train_depth: radiance
                       // gathered before bounce k reflected anything (x < 0: unset)
 };
@@ -418,7 +420,18 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                 bool queried = false;
                 if (NRC) {
                     v3 kd = base * (1.0f - m.b.x);
-                    if (!tag && (int)depth == P.query_depth) {
+                    bool query = (int)depth == P.query_depth;
+                    if (P.query_depth < 0 && !tag) {
+                        // Path spread (Mueller et al. 2021, sec. 5): a0 = t1^2 / (4 pi cos1)
+                        // at the first vertex; later vertices add sqrt(t^2 / (pdf cos)); the
+                        // path queries at vertex 2 or later once (sum)^2 > c a0.
+                        const float cv = fmaxf(fabsf(dot(ns, wo)), 1e-6f);
+                        float2 sp = depth == 0 ? make_float2(0.0f, h.x * h.x / (4.0f * kPi * cv)) : W.spread[s];
+                        if (depth > 0) sp.x += sqrtf(h.x * h.x / (fmaxf(pdf_b, 1e-12f) * cv));
+                        query = depth > 0 && sp.x * sp.x > P.spread_c * sp.y;
+                        W.spread[s] = sp;
+                    }
+                    if (!tag && query) {
                         uint32_t k = warp_append(&W.counters[kCntQuery], true);
                         W.q_pix[k] = make_float4(__int_as_float((int)pixel), thr.x, thr.y, thr.z);
                         nrc_raw(W.q_raw + 16 * (size_t)k, p, wo, ns, m.b.y, kd, B.F0);
@@ -971,7 +984,7 @@ static void ensure_nrc_workspace(aqua_ctx* ctx, size_t queries, size_t records, 
     size_t o_qp = take(16 * queries), o_qr = take(64 * queries), o_qx = take(128 * queries),
            o_qo = take(12 * queries), o_rec = take(96 * records), o_lt = take(16 * records),
            o_tr = take(64 * records), o_tx = take(128 * records), o_tt = take(12 * records),
-           o_sn = take(16 * records * snaps);
+           o_sn = take(16 * records * snaps), o_sp = take(8 * queries);
     dev_alloc(ctx, w.block, off);
     char* b = (char*)w.block.ptr;
     w.q_pix = (float4*)(b + o_qp);
@@ -984,6 +997,7 @@ static void ensure_nrc_workspace(aqua_ctx* ctx, size_t queries, size_t records, 
     w.t_x = (uint16_t*)(b + o_tx);
     w.t_target = (float*)(b + o_tt);
     w.lsnap = (float4*)(b + o_sn);
+    w.spread = (float2*)(b + o_sp);  // one per path slot (slots <= queries)
     w.queries = queries;
     w.records = records;
     w.snaps = snaps;
@@ -1014,8 +1028,11 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     ensure_workspace(ctx, slots, nb, pixels * plan.replicas);
     size_t cap_q = pixels * (size_t)cfg.spp;
     size_t cap_r = std::max<size_t>((size_t)cfg.nrc_train_samples, 1);
-    const int query_depth = cfg.visualize_cache ? 0 : std::max(0, cfg.nrc_query_vertex - 1);
-    const int train_span = std::max(1, cfg.max_depth - query_depth);
+    // nrc_query_vertex = AQUA_NRC_QUERY_SPREAD: query where the path spread
+    // exceeds c a0 (at vertex 2 or later); targets then span max_depth - 1.
+    const bool by_spread = !cfg.visualize_cache && cfg.nrc_query_vertex == AQUA_NRC_QUERY_SPREAD;
+    const int query_depth = cfg.visualize_cache ? 0 : by_spread ? -1 : std::max(0, cfg.nrc_query_vertex - 1);
+    const int train_span = std::max(1, cfg.max_depth - (by_spread ? 1 : query_depth));
     const int train_depth = std::min(cfg.max_depth + train_span, 250);
     ensure_nrc_workspace(ctx, cap_q, cap_r, (size_t)train_depth);
     Workspace& w = ctx->ws;
@@ -1040,6 +1057,7 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     P.pixels = (uint32_t)pixels;
     P.nb = (uint32_t)nb;
     P.query_depth = query_depth;
+    P.spread_c = 0.01f;  // Mueller et al. 2021
     // Fraction of paths that train: aimed at nrc_train_samples records per
     // frame (first frame: assume 3 recorded vertices per training path).
     double frac = 0.0;
@@ -1058,6 +1076,7 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     W.bucket = w.bucket; W.sh_o = w.sh_o; W.sh_d = w.sh_d; W.sh_c = w.sh_c; W.film = w.film;
     W.counters = w.counters; W.stats = w.stats;
     W.q_pix = nw.q_pix; W.q_raw = nw.q_raw; W.rec = nw.rec; W.ltrain = nw.ltrain; W.lsnap = nw.lsnap;
+    W.spread = nw.spread;
 
     auto trace_k = sorted ? k_trace_ext<true, false> : k_trace_ext<false, false>;
     auto shade_k = S.mext ? (sorted ? k_shade<true, true, true> : k_shade<false, true, true>)

@@ -172,14 +172,15 @@ def cpu_sample_run(threads: int, target_s: float, seed: int = 0):
 NRC_WORKLOAD = {"workload": "interior-1920x1080-1spp-per-frame-cache-vs-plain",
                 "scene": "synthetic interior: 153 meshes, 1.15M triangles, 8 textures 2048^2, 16 quad lights, seed 0",
                 "width": 1920, "height": 1080, "max_depth": 8, "rr_depth": 3, "frame_spp": 1,
-                "train_records_per_frame": 65536, "batch": 16384, "learning_rate": 1e-2, "query_vertex": 4,
+                "train_records_per_frame": 65536, "batch": 16384, "learning_rate": 1e-2, "query_vertex": -1,
                 "burn_in_frames": 16, "target_relmse": 1e-3, "ema_decay": 0.0, "plain_spp_per_call": 16,
                 "reference_spp": 65536, "reference_rows": "rows 8, 24, ..., 1064 (every 16th row, 67 rows)",
                 "error_rows": "the reference's rows: relMSE over every 16th row, an unbiased estimate of the "
                               "whole image's relMSE",
                 "note": "cached renderer: 1 spp per 1920x1080 frame, online training on 65,536 records per frame "
-                        "(Adam, lr 1e-2), queried at vertex 4 (allowed: vertex >= 2), frames after the burn-in "
-                        "averaged; plain: the wavefront path tracer at 16 spp per call; both render whole frames "
+                        "(Adam, lr 1e-2), queried where the path spread first exceeds 0.01 x the first-hit "
+                        "footprint, at vertex >= 2 (query_vertex -1; fixed vertices 2..5 measured 0.67-0.87x), "
+                        "frames after the burn-in averaged; plain: the wavefront path tracer at 16 spp per call; both render whole frames "
                         "and are timed by wall clock per call (error evaluation excluded)"}
 REF_ROW_BEGIN, REF_ROW_STEP = 8, 16
 
@@ -771,9 +772,10 @@ def main():
     ap.add_argument("--no-interior", action="store_true", help="skip the 1080p interior measurement")
     # dram__bytes_read.sum + dram__bytes_write.sum of one full-queue
     # k_trace_ext launch (1M rays) of this workload, from `ncu --set full`
-    # (41.53 MB read + 4.16 MB written); every launch of the step has the
-    # same queue size until the last samples drain.
-    ap.add_argument("--traffic-per-launch", type=float, default=45.70e6,
+    # (40.53 MB read + 3.00 MB written,
+    # profiles/wavefront_iteration_cornell-ggx-1024x1024.md); every launch of
+    # the step has the same queue size until the last samples drain.
+    ap.add_argument("--traffic-per-launch", type=float, default=43.53e6,
                     help="DRAM bytes per k_trace_ext launch from an ncu capture")
     ap.add_argument("--spp", type=int, default=0,
                     help="samples per pixel of the workload (default 1024; smaller only for profiling captures)")

@@ -91,6 +91,7 @@ typedef struct aqua_trace_counts {
  * batch_size, max_depth, training_iters, learning_rate, visualize_cache),
  * plus the knobs the render path needs. */
 enum { AQUA_INTEGRATOR_PATH = 0, AQUA_INTEGRATOR_NRC = 1 };
+enum { AQUA_NRC_QUERY_SPREAD = -1 };
 
 typedef struct aqua_integrator_cfg {
     int32_t type;            /* AQUA_INTEGRATOR_PATH or AQUA_INTEGRATOR_NRC */
@@ -106,7 +107,11 @@ typedef struct aqua_integrator_cfg {
     uint64_t seed;           /* RNG seed: PCG32 stream per pixel            */
     int32_t spp_offset;      /* first sample index (progressive rendering)  */
     int32_t nrc_train_samples; /* NRC: training records per frame          */
-    int32_t nrc_query_vertex;  /* NRC: query the cache at this vertex (>= 2; default 4) */
+    int32_t nrc_query_vertex;  /* NRC: query the cache at this vertex (>= 2),
+                                  or AQUA_NRC_QUERY_SPREAD (the default):
+                                  where the path's spread first exceeds 0.01 x
+                                  its first-hit footprint (Mueller et al.
+                                  2021), at vertex 2 or later */
     /* Row subset (wavefront renders): with row_step > 1 only the camera
      * image's rows row_begin, row_begin + row_step, ... are rendered, and
      * rgb_out holds just those rows in order (rows x width x 3). Every pixel
@@ -464,7 +469,8 @@ AQUA_API aqua_status aqua_nrc_train_step(aqua_ctx* ctx, aqua_nrc* nrc, const uin
 
 /* One frame of the cached renderer (`"type": "nrc"`, integrator.json:2).
  * cfg->spp samples per pixel. Paths stop at vertex cfg->nrc_query_vertex
- * (vertex 1 = first hit) and add throughput x cache; about
+ * (vertex 1 = first hit), or where their spread calls for it
+ * (AQUA_NRC_QUERY_SPREAD), and add throughput x cache; about
  * cfg->nrc_train_samples vertices of unbiased training paths become
  * training records, and the network takes ceil(records / cfg->batch_size)
  * Adam steps (at most cfg->training_iters when that is > 0) after the frame

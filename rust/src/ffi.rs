@@ -26,6 +26,7 @@ pub const AQUA_ERR_TIMEOUT: aqua_status = 7;
 pub const AQUA_ERR_UNSUPPORTED: aqua_status = 8;
 
 pub const AQUA_VERSION: c_int = 300;  // compare with aqua_version() at start-up
+pub const AQUA_NRC_QUERY_SPREAD: i32 = -1;
 pub const AQUA_BVH_AUTO: i32 = -1;
 pub const AQUA_BVH_FULL: i32 = 0;
 pub const AQUA_BVH_QUANTIZED: i32 = 1;

@@ -147,3 +147,27 @@ def test_cached_render_converges_and_gains(gpu_ctx, trained):
     plain, _ = gpu_ctx.render(s, gpu_ctx.integrator(spp=64, max_depth=8, rr_depth=3, seed=7000))
     e_cached, e_plain = rel_mse(cached, ref), rel_mse(plain, ref)
     assert e_cached < 0.8 * e_plain, (e_cached, e_plain)
+
+
+def test_path_spread_query_lies_between_the_fixed_cuts(gpu_ctx):
+    """AQUA_NRC_QUERY_SPREAD queries where a path's spread exceeds 0.01 of its
+    first-hit footprint, at vertex 2 or later. With a zero network every path
+    is the path tracer's, with the same random numbers, cut at its query
+    vertex: per pixel the image lies between the path tracer cut at vertex 2
+    and the uncut path tracer, and the GGX box's glossy hits (small spread)
+    make it differ from the vertex-2 cut."""
+    import aqua
+
+    s = gpu_ctx.procedural(2, seed=0, width=48, height=40)
+    net = aqua.Nrc(gpu_ctx, seed=1)
+    net.set_weights(np.zeros(20672, np.float32))
+    img, st = gpu_ctx.render_nrc(s, nrc_cfg(gpu_ctx, spp=16, seed=5, nrc_query_vertex=aqua.NRC_QUERY_SPREAD), net)
+    cut2, _ = gpu_ctx.render_nrc(s, nrc_cfg(gpu_ctx, spp=16, seed=5, nrc_query_vertex=2), net)
+    full, _ = gpu_ctx.render(s, gpu_ctx.integrator(spp=16, max_depth=8, rr_depth=3, seed=5),
+                             tuning=gpu_ctx.tuning(replicas=1))
+    eps = 1e-5 * (1.0 + full)
+    assert np.all(img >= cut2 - eps) and np.all(img <= full + eps)
+    assert np.mean(np.abs(img - cut2) > 1e-6) > 0.01
+    assert 0 < st.nrc_queries <= 48 * 40 * 16
+    net.free()
+    s.free()
