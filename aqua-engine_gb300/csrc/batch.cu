@@ -228,7 +228,7 @@ __device__ __forceinline__ bool shade_hit(const DevScene& S, int max_depth, int 
 // 4 resident blocks of 256 (64 registers): the spilled path state costs less
 // than the latency the extra warps hide (measured on the 64-job batch: 48,
 // 64 and 80 registers and the compiler's own 107 compared).
-template <bool FULL>
+template <bool FULL, int NODES>
 __global__ void __launch_bounds__(256, 4) k_batch(const DevScene* __restrict__ scenes, const DevJob* __restrict__ jobs, int njobs,
                         uint32_t total_pixels, uint32_t* __restrict__ counters,
                         unsigned long long* __restrict__ clocks, unsigned long long* __restrict__ stats) {
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(256, 4) k_batch(const DevScene* __restrict__ s
         const bool any = P.shadow;
         if (any) ++n_sh;
         else ++n_ext;
-        const TraceResult h = traverse_fast(S, (FULL && any) ? P.so : P.o, any ? P.sdir : P.dir, 0.0f,
+        const TraceResult h = traverse_fast<NODES>(S, (FULL && any) ? P.so : P.o, any ? P.sdir : P.dir, 0.0f,
                                             any ? P.stmax : INFINITY, any);
         bool alive;
         if (any) {
@@ -358,7 +358,10 @@ static BatchResult launch_jobs(aqua_ctx* ctx, std::vector<DevJob>& jobs, std::ve
     if (block != 64 && block != 128 && block != 256) throw Error(AQUA_ERR_INVALID_ARG, "block size must be 64, 128 or 256");
     bool full = false;  // some scene's materials set the full model's lobes
     for (const DevScene& sc : scenes) full = full || sc.mext != nullptr;
-    auto kernel = full ? k_batch<true> : k_batch<false>;
+    bool qbvh = false;  // some scene walks quantized nodes
+    for (const DevScene& sc : scenes) qbvh = qbvh || sc.qbvh != 0;
+    auto kernel = full ? (qbvh ? k_batch<true, kNodesAny> : k_batch<true, kNodesFull>)
+                       : (qbvh ? k_batch<false, kNodesAny> : k_batch<false, kNodesFull>);
     int per_sm = tune.blocks_per_sm;
     if (per_sm <= 0) {
         AQ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0));

@@ -164,9 +164,17 @@ __device__ __forceinline__ int32_t visit_quantized(const DevScene& S, int32_t no
     return sp > 0 ? stack[--sp] : kTraversalDone;
 }
 
-// One node visit in the scene's node format (warp-uniform branch).
+// Node formats a walk is compiled for: full-precision only, or either
+// (the scene's, a warp-uniform branch). Kernels whose instruction cache is
+// tight (the batch kernel) take the full-precision walk alone unless one of
+// their scenes holds quantized nodes.
+enum { kNodesFull = 0, kNodesAny = 1 };
+
+// One node visit in the scene's node format.
+template <int NODES = kNodesAny>
 __device__ __forceinline__ int32_t visit_node(const DevScene& S, int32_t node, const RayPre& rp, float tfar,
                                               int32_t* stack, int& sp) {
+    if (NODES == kNodesFull) return visit_wide(S, node, rp, tfar, stack, sp);
     return S.qbvh ? visit_quantized(S, node, rp, tfar, stack, sp) : visit_wide(S, node, rp, tfar, stack, sp);
 }
 
@@ -230,6 +238,7 @@ __device__ __forceinline__ TraceResult traverse(const DevScene& S, v3 o, v3 d, f
 // the order of visits, and thus the work counts, differ. `any` (stop at the
 // first hit) is a run-time flag, so a kernel that traces both kinds of ray
 // from one call site holds one inlined copy of the walk.
+template <int NODES = kNodesAny>
 __device__ __forceinline__ TraceResult traverse_fast(const DevScene& S, v3 o, v3 d, float tmin, float tmax,
                                                      bool any) {
     RayPre rp;
@@ -245,7 +254,7 @@ __device__ __forceinline__ TraceResult traverse_fast(const DevScene& S, v3 o, v3
     int32_t node = 0, leaf = 0;
     while (true) {
         while (node >= 0) {
-            node = visit_node(S, node, rp, r.t, stack, sp);
+            node = visit_node<NODES>(S, node, rp, r.t, stack, sp);
             if (node < 0 && node != kTraversalDone && leaf == 0) {
                 leaf = node;
                 node = sp > 0 ? stack[--sp] : kTraversalDone;
