@@ -615,10 +615,16 @@ Closest<double> closest<double>(const orc_scene* s, V3<double> o, V3<double> d, 
 // Optional constant radiance cache: paths stop at bounce query_depth and
 // add throughput x cache_rgb (the device's cache query with a network whose
 // output is that constant).
+// query_depth -2: the path-spread rule instead of a fixed bounce (Mueller et
+// al. 2021, sec. 5; the device's AQUA_NRC_QUERY_SPREAD): a0 = t1^2 / (4 pi
+// cos1) at the first vertex, the spread grows by sqrt(t^2 / (pdf cos)) per
+// later vertex, and the path queries at the first vertex from bounce 1 on
+// where spread^2 > 0.01 a0 (cos against the shading normal).
 struct CacheConst {
     int query_depth = -1;
     double rgb[3] = {0, 0, 0};
 };
+constexpr int kQuerySpread = -2;
 
 template <class T>
 void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>& cdf, int32_t spp, int32_t spp_offset,
@@ -654,6 +660,7 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
         V3<T> d = unit(R * dc.x + U * dc.y + B * dc.z);
         V3<T> thr{1, 1, 1};
         T pdf_b = 0;
+        T spread = 0, a0 = 0;  // path-spread query mode
         for (int depth = 0;; ++depth) {
             st[1] += 1;
             Closest<T> h = closest<T>(s, o, d, inf, false);
@@ -703,6 +710,15 @@ void render_pixel(const orc_scene* s, const Lut& lut, const std::vector<double>&
                     n = n * (T(1) / std::sqrt(l2));
                     if (dot3(n, ng) < T(0)) n = -n;
                     if (dot3(n, wo) > T(0)) ns = n;
+                }
+            }
+            if (cache.query_depth == kQuerySpread) {
+                const T cv = std::max(std::fabs(dot3(ns, wo)), T(1e-6));
+                if (depth == 0) a0 = h.t * h.t / (T(4) * T(M_PI) * cv);
+                else spread += std::sqrt(h.t * h.t / (std::max(pdf_b, T(1e-12)) * cv));
+                if (depth > 0 && spread * spread > T(0.01) * a0) {
+                    for (int c2 = 0; c2 < 3; ++c2) sum[c2] += (double)at(thr, c2) * cache.rgb[c2];
+                    break;
                 }
             }
             const aqua_material& m = s->mats[s->tri_mat[h.id]];

@@ -83,7 +83,9 @@ int orc_render_pixels(const orc_scene* s, int precision, int32_t spp, int32_t sp
                       double* stats);
 
 /* As orc_render, with a constant radiance cache: every path stops at bounce
- * query_depth (0 = first hit) and adds throughput x cache_rgb there. */
+ * query_depth (0 = first hit) and adds throughput x cache_rgb there;
+ * query_depth -2 queries by the path-spread rule instead (the device's
+ * AQUA_NRC_QUERY_SPREAD: from bounce 1 on, where spread^2 > 0.01 a0). */
 int orc_render_cached(const orc_scene* s, int precision, int32_t spp, int32_t spp_offset, int32_t max_depth,
                       int32_t rr_depth, uint64_t seed, int threads, int64_t pixel_begin, int64_t pixel_end,
                       int32_t query_depth, const float* cache_rgb, float* out, double* stats);

@@ -171,3 +171,25 @@ def test_path_spread_query_lies_between_the_fixed_cuts(gpu_ctx):
     assert 0 < st.nrc_queries <= 48 * 40 * 16
     net.free()
     s.free()
+
+
+@pytest.mark.parametrize("config", [2, 3])
+def test_path_spread_constant_cache_matches_oracle(gpu_ctx, config):
+    """The path-spread query rule against the FP64 oracle's restatement of
+    it (query_depth -2), with a constant network: the same vertices query,
+    sample for sample (the rule reads the hit distance, the shading normal
+    and the previous bounce's pdf, which the oracle computes in double)."""
+    import aqua
+    import pyoracle
+
+    rgb = [0.25, 0.5, 0.125]  # exact in bf16
+    s = gpu_ctx.procedural(config, seed=0, width=40, height=32)
+    o = pyoracle.OracleScene.from_aqua(s)
+    net = aqua.Nrc(gpu_ctx, seed=1)
+    net.set_weights(constant_weights(rgb))
+    img, st = gpu_ctx.render_nrc(s, nrc_cfg(gpu_ctx, spp=64, seed=9, nrc_query_vertex=aqua.NRC_QUERY_SPREAD), net)
+    ref, _ = o.render(64, 8, seed=9, precision=64, query_depth=-2, cache_rgb=rgb)
+    assert rel_mse(img, ref) < TOL
+    assert st.nrc_queries > 0
+    net.free()
+    s.free()
