@@ -333,9 +333,10 @@ SPHERES_WORKLOAD = {"workload": "sphere-field-1024x1024-64spp-depth8", "width": 
 # captures of these scenes, and the rays that launch traced.
 TRACE_TRAFFIC = {
     "interior": {"bytes": 564.4e6, "rays": 2073600,
-                 "source": "profiles/trace_interior-1920x1080-256spp.md (497.3 MB read + 67.1 MB written)"},
+                 "source": "ncu capture of a full-queue launch inside a 1080p interior render "
+                           "(497.3 MB read + 67.1 MB written)"},
     "spheres": {"bytes": 180.36e6, "rays": 1048576,
-                "source": "profiles/trace_sphere-field-1024x1024.md (172.6 MB read + 7.7 MB written, the render's "
+                "source": "ncu capture of the sphere field (172.6 MB read + 7.7 MB written, the render's "
                           "third launch: full queue of camera and first-bounce rays)"},
 }
 
@@ -752,6 +753,40 @@ def run_profile_scene(args):
     ctx.close()
 
 
+def run_profile_cache_frame(args):
+    """Profiling hook: the cached renderer on the config-4 workload (interior
+    1920x1080, 1 spp per frame, online training): 20 warm-up frames, then one
+    frame inside the NVTX range "cache_frame"; prints the frame's wall and
+    network times."""
+    import torch
+    import aqua
+
+    W = NRC_WORKLOAD
+    ctx = aqua.Context(device=0)
+    scene = ctx.procedural(3, seed=0, width=W["width"], height=W["height"])
+    film = torch.zeros((W["height"], W["width"], 3), dtype=torch.float32, device="cuda")
+    net = aqua.Nrc(ctx, seed=1, learning_rate=W["learning_rate"])
+    cfg = lambda f: ctx.integrator(type=aqua.INTEGRATOR_NRC, spp=W["frame_spp"], max_depth=W["max_depth"],
+                                   rr_depth=W["rr_depth"], seed=1000 + f, nrc_query_vertex=W["query_vertex"],
+                                   nrc_train_samples=W["train_records_per_frame"], batch_size=W["batch"],
+                                   training_iters=0)
+    for f in range(20):
+        ctx.render_nrc(scene, cfg(f), net, dev_ptr=film.data_ptr())
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("cache_frame")
+    t0 = time.perf_counter()
+    _, st = ctx.render_nrc(scene, cfg(20), net, dev_ptr=film.data_ptr())
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    torch.cuda.nvtx.range_pop()
+    log(json.dumps({"frame_ms": wall * 1e3, "device_ms": st.device_ms, "nrc_ms": st.nrc_ms,
+                    "iterations": st.iterations, "launches": st.total_launches, "queries": st.nrc_queries,
+                    "records": st.nrc_train_records}))
+    net.free()
+    scene.free()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -772,20 +807,24 @@ def main():
     ap.add_argument("--no-interior", action="store_true", help="skip the 1080p interior measurement")
     # dram__bytes_read.sum + dram__bytes_write.sum of one full-queue
     # k_trace_ext launch (1M rays) of this workload, from `ncu --set full`
-    # (40.53 MB read + 3.00 MB written,
-    # profiles/wavefront_iteration_cornell-ggx-1024x1024.md); every launch of
-    # the step has the same queue size until the last samples drain.
+    # (40.53 MB read + 3.00 MB written, iteration 2 of a 16-spp render); every
+    # launch of the step has the same queue size until the last samples drain.
     ap.add_argument("--traffic-per-launch", type=float, default=43.53e6,
                     help="DRAM bytes per k_trace_ext launch from an ncu capture")
     ap.add_argument("--spp", type=int, default=0,
                     help="samples per pixel of the workload (default 1024; smaller only for profiling captures)")
     ap.add_argument("--profile-scene", type=int, default=0, choices=[0, 2, 3, 5],
                     help="profiling hook: render one scene once (with --spp) and exit")
+    ap.add_argument("--profile-cache-frame", action="store_true",
+                    help="profiling hook: one cached-renderer frame of the config-4 workload, then exit")
     ap.add_argument("--profile-train", type=int, default=0,
                     help="profiling hook: time cache training steps on this many rows and exit")
     args = ap.parse_args()
     if args.profile_scene:
         run_profile_scene(args)
+        return
+    if args.profile_cache_frame:
+        run_profile_cache_frame(args)
         return
     if args.profile_train:
         import aqua
