@@ -333,18 +333,55 @@ __global__ void k_nrc_adam(const float* __restrict__ partial, int chunks, float*
 }
 
 // ---------------------------------------------------------------- encoding
-__global__ void k_nrc_encode(const float* __restrict__ raw, int n, float3 bmin, float3 binv,
-                             uint16_t* __restrict__ X) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    NrcRaw r;
-    memcpy(&r, raw + (size_t)i * kNrcRaw, sizeof(NrcRaw));
-    float pn[3] = {nrc_wrap01((r.p[0] - bmin.x) * binv.x), nrc_wrap01((r.p[1] - bmin.y) * binv.y),
-                   nrc_wrap01((r.p[2] - bmin.z) * binv.z)};
-    uint32_t* out = reinterpret_cast<uint32_t*>(X + (size_t)i * 64);
-    for (int c = 0; c < 64; c += 2)
-        out[c / 2] = (uint32_t)bf16_bits(nrc_encode_one(r, pn, c)) |
-                     ((uint32_t)bf16_bits(nrc_encode_one(r, pn, c + 1)) << 16);
+// A block encodes 128 rows. Raw rows come in and encoded rows go out through
+// shared memory so that both move as contiguous, coalesced words (a thread's
+// own row is 64 B in and 128 B out: one row per thread would touch a line
+// per lane and word). Each row's spherical coordinates are computed once and
+// each position octave with one sincospif of the exactly scaled coordinate.
+constexpr int kEncRows = 128;
+
+__device__ __forceinline__ uint32_t bf16_pair(float lo, float hi) {
+    return (uint32_t)bf16_bits(lo) | ((uint32_t)bf16_bits(hi) << 16);
+}
+
+__global__ void __launch_bounds__(kEncRows) k_nrc_encode(const float* __restrict__ raw, int n, float3 bmin,
+                                                         float3 binv, uint16_t* __restrict__ X) {
+    __shared__ float s_raw[kEncRows][kNrcRaw + 1];  // +1: conflict-free row reads
+    __shared__ uint32_t s_out[kEncRows][33];
+    const int t = threadIdx.x;
+    const size_t row0 = (size_t)blockIdx.x * kEncRows;
+    const int rows = min(kEncRows, n - (int)row0);
+    const float* src = raw + row0 * kNrcRaw;
+    for (int k = t; k < rows * kNrcRaw; k += kEncRows) s_raw[k / kNrcRaw][k % kNrcRaw] = src[k];
+    __syncthreads();
+    if (t < rows) {
+        const float* r = s_raw[t];
+        uint32_t* o = s_out[t];
+        float pn[3] = {nrc_wrap01((r[0] - bmin.x) * binv.x), nrc_wrap01((r[1] - bmin.y) * binv.y),
+                       nrc_wrap01((r[2] - bmin.z) * binv.z)};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int f = 0; f < 8; ++f) {
+                float sn, cs;
+                sincospif(pn[a] * (float)(1 << f), &sn, &cs);  // the scale by 2^f is exact
+                o[a * 8 + f] = bf16_pair(sn, cs);
+            }
+        float du, dv, nu, nv;
+        sph01(r[3], r[4], r[5], du, dv);
+        sph01(r[6], r[7], r[8], nu, nv);
+        o[24] = bf16_pair(one_blob(du, 0, 3), one_blob(du, 1, 3));
+        o[25] = bf16_pair(one_blob(du, 2, 3), one_blob(dv, 0, 3));
+        o[26] = bf16_pair(one_blob(dv, 1, 3), one_blob(dv, 2, 3));
+        o[27] = bf16_pair(one_blob(nu, 0, 2), one_blob(nu, 1, 2));
+        o[28] = bf16_pair(one_blob(nv, 0, 2), one_blob(nv, 1, 2));
+        o[29] = bf16_pair(nrc_wrap01(r[9]), r[10]);
+        o[30] = bf16_pair(r[11], r[12]);
+        o[31] = bf16_pair(0.2126f * r[13] + 0.7152f * r[14] + 0.0722f * r[15], 1.0f);
+    }
+    __syncthreads();
+    uint32_t* dst = reinterpret_cast<uint32_t*>(X + row0 * kNrcIn);
+    for (int k = t; k < rows * 32; k += kEncRows) dst[k] = s_out[k >> 5][k & 31];
 }
 
 // ---------------------------------------------------------------- host side
@@ -504,7 +541,7 @@ void nrc_encode_dev(aqua_ctx* ctx, NrcNet& net, const float* raw, int n, uint16_
     if (n <= 0) return;
     float3 bmin = make_float3(net.bmin[0], net.bmin[1], net.bmin[2]);
     float3 binv = make_float3(1.0f / net.bext[0], 1.0f / net.bext[1], 1.0f / net.bext[2]);
-    k_nrc_encode<<<(n + 127) / 128, 128, 0, ctx->stream>>>(raw, n, bmin, binv, X);
+    k_nrc_encode<<<(n + kEncRows - 1) / kEncRows, kEncRows, 0, ctx->stream>>>(raw, n, bmin, binv, X);
     AQ_CUDA(cudaGetLastError());
 }
 

@@ -60,29 +60,4 @@ AQ_HD void sph01(float x, float y, float z, float& u, float& v) {
     v = nrc_wrap01(v);
 }
 
-// Encoded value c (0..63) of a vertex; pn = position normalised to [0,1]^3.
-AQ_HD float nrc_encode_one(const NrcRaw& r, const float pn[3], int c) {
-    if (c < 48) {
-        int axis = c / 16, f = (c % 16) / 2;
-        float x = pn[axis] * (float)(1 << f) * kPi;
-        return (c & 1) ? cosf(x) : sinf(x);
-    }
-    if (c < 54) {
-        float u, v;
-        sph01(r.w[0], r.w[1], r.w[2], u, v);
-        int k = c - 48;
-        return one_blob(k < 3 ? u : v, k % 3, 3);
-    }
-    if (c < 58) {
-        float u, v;
-        sph01(r.n[0], r.n[1], r.n[2], u, v);
-        int k = c - 54;
-        return one_blob(k < 2 ? u : v, k & 1, 2);
-    }
-    if (c == 58) return nrc_wrap01(r.rough);
-    if (c < 62) return r.kd[c - 59];
-    if (c == 62) return 0.2126f * r.ks[0] + 0.7152f * r.ks[1] + 0.0722f * r.ks[2];
-    return 1.0f;
-}
-
 }  // namespace aq
