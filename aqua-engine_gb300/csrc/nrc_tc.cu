@@ -3,10 +3,10 @@
 // by TMA.
 //
 // One persistent CTA per SM holds the network's bf16 weights (42 KB) in shared
-// memory once and runs kTcGroups independent warpgroups. A warpgroup owns 128
-// TMEM columns (64 for the FP32 accumulator, 32 for the next layer's bf16
-// activations) and a 128-row input tile in shared memory, and works through
-// its tiles alone:
+// memory once and runs kTcFwdGroups independent warpgroups. A warpgroup owns
+// 96 TMEM columns (64 for the FP32 accumulator, 32 for the next layer's bf16
+// activations; five groups fill 480 of the SM's 512) and a 128-row input
+// tile in shared memory, and works through its tiles alone:
 //   - its first thread loads the next input tile with TMA (eight 128 x 8-column
 //     boxes) as soon as layer 1 has read the current one;
 //   - per layer the same thread issues four tcgen05.mma.kind::f16 (M = 128,
@@ -42,23 +42,29 @@
 namespace aq {
 
 constexpr int kTcRows = 128;                      // rows per tile (MMA M)
-constexpr int kTcGroups = 4;                      // warpgroups (tiles in flight) per CTA
+constexpr int kTcGroups = 4;                      // warpgroups (tiles in flight) per CTA, training kernels
 constexpr int kTcThreads = 128 * kTcGroups;
 constexpr int kTcTileBytes = kTcRows * 64 * 2;    // 16 KB per input or activation tile
 constexpr int kTcLayerBytes = 64 * 64 * 2;        // 8 KB hidden-layer weights
 constexpr int kTcOutRows = 16;                    // output layer padded to N = 16 (3 used)
 constexpr int kTcOutBytes = kTcOutRows * 64 * 2;  // 2 KB
 constexpr int kTcWeightBytes = 5 * kTcLayerBytes + kTcOutBytes;  // 42 KB
-// The input tiles need 106 KB; asking for 120 KB keeps two CTAs (and two
-// full TMEM allocations) off one SM.
-constexpr int kTcSmemBytes = std::max(kTcWeightBytes + kTcGroups * kTcTileBytes + 1024, 120 * 1024);
 constexpr uint32_t kTcGroupCols = 128;            // accumulator 64 + activations 32, rounded up
 constexpr uint32_t kTcActCol = 64;                // activation columns within a group
 constexpr uint32_t kTcTmemCols = kTcGroupCols * kTcGroups;  // a power of two >= 32
 constexpr uint32_t kTcWaitLimit = 1u << 22;       // try_wait rounds before a wait gives up
+// Inference: five groups (tiles in flight; four measured 9% slower),
+// accumulators at columns 64 g, activations after all accumulators at
+// 64 * 5 + 32 g. The weights and five input tiles take 123 KB of shared
+// memory, which keeps two CTAs (and two full TMEM allocations) off one SM.
+constexpr int kTcFwdGroups = 5;
+constexpr int kTcFwdThreads = 128 * kTcFwdGroups;
+constexpr int kTcFwdSmemBytes = std::max(kTcWeightBytes + kTcFwdGroups * kTcTileBytes + 1024, 120 * 1024);
+constexpr uint32_t kTcFwdActBase = 64u * kTcFwdGroups;
+static_assert(kTcFwdActBase + 32u * kTcFwdGroups <= kTcTmemCols, "inference TMEM columns");
+static_assert(kTcFwdSmemBytes <= 227 * 1024, "shared memory per CTA");
 static_assert((kTcTmemCols & (kTcTmemCols - 1)) == 0 && kTcTmemCols >= 32 && kTcTmemCols <= 512, "TMEM alloc");
 static_assert(kTcWeightBytes % 1024 == 0 && kTcTileBytes % 1024 == 0, "tiles stay 1024-byte aligned");
-static_assert(kTcSmemBytes <= 227 * 1024, "shared memory per CTA");
 
 // Byte offset of element (r, k) in an R-row operand tile.
 __host__ __device__ constexpr uint32_t tc_offset(int rows, int r, int k) {
@@ -212,11 +218,11 @@ __device__ __forceinline__ uint32_t relu_pack2(uint32_t lo, uint32_t hi) {
 // X (through `xmap`): n rows x 64 bf16; out: n x 3 fp32; err: set to 1 when a
 // wait expired. acts (training, may be null): the hidden activations H1..H5
 // as bf16 rows, acts[l][row][64], for the backward pass.
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kTcFwdThreads, 1)
     k_nrc_forward_tc(const __grid_constant__ CUtensorMap xmap, int n, const uint4* __restrict__ wimg,
                      float* __restrict__ out, uint32_t* __restrict__ err, uint4* __restrict__ acts) {
     extern __shared__ uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t bar_in[kTcGroups], bar_mma[kTcGroups];
+    __shared__ __align__(8) uint64_t bar_in[kTcFwdGroups], bar_mma[kTcFwdGroups];
     __shared__ uint32_t tmem_base_slot;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -226,8 +232,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const uint32_t sW = base;
     const uint32_t sI = base + kTcWeightBytes + (uint32_t)g * kTcTileBytes;  // this group's input tile
 
-    for (int i = tid; i < kTcWeightBytes / 16; i += kTcThreads) reinterpret_cast<uint4*>(sbase)[i] = wimg[i];
-    if (tid < kTcGroups) {
+    for (int i = tid; i < kTcWeightBytes / 16; i += kTcFwdThreads) reinterpret_cast<uint4*>(sbase)[i] = wimg[i];
+    if (tid < kTcFwdGroups) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar_in[tid])) : "memory");
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar_mma[tid])) : "memory");
     }
@@ -247,13 +253,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     tc_fence_after();
 
-    const uint32_t tmem = tmem_base_slot + (uint32_t)g * kTcGroupCols;   // this group's accumulator
-    const uint32_t tact = tmem + kTcActCol;                              // and activations
-    const uint32_t lanes = (uint32_t)(q * 32) << 16;                     // this warp's lanes
+    const uint32_t tmem = tmem_base_slot + (uint32_t)g * 64u;                    // this group's accumulator
+    const uint32_t tact = tmem_base_slot + kTcFwdActBase + (uint32_t)g * 32u;   // and activations
+    const uint32_t lanes = (uint32_t)(q * 32) << 16;                             // this warp's lanes
     const uint32_t mb_in = smem_u32(&bar_in[g]), mb_mma = smem_u32(&bar_mma[g]);
     const int bar_id = 1 + g;
     const int tiles = (n + kTcRows - 1) / kTcRows;
-    const int stride = (int)gridDim.x * kTcGroups;
+    const int stride = (int)gridDim.x * kTcFwdGroups;
     const int row = q * 32 + lane;  // TMEM lane = tile row
     uint32_t ph_in = 0, ph_mma = 0;      // parity of the next phase to wait for
     uint32_t tma_par = 0, mma_par = 0;   // parity the work in flight will complete
@@ -588,12 +594,12 @@ void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n
                                       CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw Error(AQUA_ERR_CUDA, "cuTensorMapEncodeTiled failed for the query rows");
     if (!ctx->nrc_tc_ready) {  // once per context (one device)
-        AQ_CUDA(cudaFuncSetAttribute(k_nrc_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes));
+        AQ_CUDA(cudaFuncSetAttribute(k_nrc_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcFwdSmemBytes));
         ctx->nrc_tc_ready = true;
     }
     const int tiles = (n + kTcRows - 1) / kTcRows;
     const int grid = std::max(1, std::min(tiles, ctx->num_sms));
-    k_nrc_forward_tc<<<grid, kTcThreads, kTcSmemBytes, ctx->stream>>>(map, n, reinterpret_cast<const uint4*>(img),
+    k_nrc_forward_tc<<<grid, kTcFwdThreads, kTcFwdSmemBytes, ctx->stream>>>(map, n, reinterpret_cast<const uint4*>(img),
                                                                        out, err, reinterpret_cast<uint4*>(acts));
     AQ_CUDA(cudaGetLastError());
 }
