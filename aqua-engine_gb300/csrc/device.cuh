@@ -63,6 +63,16 @@ struct TraceResult {
 template <class T>
 __device__ __forceinline__ T ldg_(const T* p) { return __ldg(p); }
 
+// Programmatic dependent launch: wait until the kernel this one was chained
+// to (launched with programmatic stream serialization) has completed and
+// its writes are visible. Returns at once for a kernel launched normally.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+// Lets the kernel chained after this one be scheduled once every block of
+// this grid has passed this point (its blocks then take SM slots as this
+// grid's blocks exit, and wait in grid_dep_wait). No effect without a
+// chained kernel.
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
 // Two consecutive 16-byte words in one 256-bit load through the read-only
 // path (sm_100 and later); p must be 32-byte aligned.
 __device__ __forceinline__ void ldg2x4(const float4* p, float4& a, float4& b) {

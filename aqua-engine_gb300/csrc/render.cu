@@ -222,6 +222,8 @@ __device__ __forceinline__ void ltrain_add(float4* L, uint32_t id, v3 c) {
 template <bool SORTED, bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_ext(DevScene S, WaveParams P, WavePtrs W, uint32_t cnt_in,
                                                    uint32_t cnt_out) {
+    grid_dep_wait();
+    grid_dep_launch();
     uint32_t n = W.counters[cnt_in];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counters[cnt_out] = 0;
@@ -301,6 +303,8 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
         float c = (float)i / 255.0f;
         lut[i] = c <= 0.04045f ? c / 12.92f : powf((c + 0.055f) / 1.055f, 2.4f);
     }
+    grid_dep_wait();
+    grid_dep_launch();
     uint32_t n;
     if (SORTED) {
         if (threadIdx.x == 0) {
@@ -559,6 +563,8 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
 
 template <bool COUNT, bool NRC = false>
 __global__ void __launch_bounds__(128) k_shadow(DevScene S, WaveParams P, WavePtrs W) {
+    grid_dep_wait();
+    grid_dep_launch();
     uint32_t n = W.counters[kCntShadow];
     if (blockIdx.x == 0) {
         for (uint32_t b = threadIdx.x; b < P.nb; b += blockDim.x) W.counters[kCntBucket0 + b] = 0;
@@ -674,6 +680,25 @@ static void ensure_workspace(aqua_ctx* ctx, size_t slots, size_t buckets, size_t
 void workspace_release(aqua_ctx* ctx) {
     dev_free(ctx->ws.block);
     ctx->ws = Workspace{};
+}
+
+// Launches kernel k chained to the previous work in stream st (programmatic
+// dependent launch): its blocks may be scheduled while the previous kernel's
+// last blocks drain, and it waits for that kernel (grid_dep_wait) before its
+// first dependent read. Hides the launch gap between the wavefront stages.
+template <class... KArgs, class... Args>
+static void launch_chained(void (*k)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)grid);
+    lc.blockDim = dim3((unsigned)block);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    AQ_CUDA(cudaLaunchKernelEx(&lc, k, args...));
 }
 
 template <class K>
@@ -853,11 +878,11 @@ void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, 
             // the events barely perturb the launch stream.
             bool timed = timing && (iter % kStageTimingStride) == 0;
             if (timed) tt.begin();
-            trace_k<<<g_trace, bt, 0, st>>>(S, P, W, in, out);
+            launch_chained(trace_k, g_trace, bt, st, S, P, W, in, out);
             if (timed) { tt.end(); ts.begin(); }
-            shade_k<<<g_shade, bs, 0, st>>>(S, P, W, in, out);
+            launch_chained(shade_k, g_shade, bs, st, S, P, W, in, out);
             if (timed) { ts.end(); tsh.begin(); }
-            shadow_k<<<g_shadow, bt, 0, st>>>(S, P, W);
+            launch_chained(shadow_k, g_shadow, bt, st, S, P, W);
             if (timed) tsh.end();
             launches += 3;
         }
@@ -1113,9 +1138,9 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
             uint32_t in = (uint32_t)(iter & 1), out = 1u - in;
             W.q_in = w.q[in];
             W.q_out = w.q[out];
-            trace_k<<<g_trace, 128, 0, st>>>(S, P, W, in, out);
-            shade_k<<<g_shade, 128, 0, st>>>(S, P, W, in, out);
-            shadow_k<<<g_shadow, 128, 0, st>>>(S, P, W);
+            launch_chained(trace_k, g_trace, 128, st, S, P, W, in, out);
+            launch_chained(shade_k, g_shade, 128, st, S, P, W, in, out);
+            launch_chained(shadow_k, g_shadow, 128, st, S, P, W);
             launches += 3;
         }
         AQ_CUDA(cudaGetLastError());
