@@ -64,6 +64,27 @@ struct EventPair {
     }
 };
 
+#if defined(__CUDACC__)
+// Launches kernel k chained to the previous work in stream st (programmatic
+// dependent launch): its blocks may be scheduled while the previous kernel's
+// last blocks drain, and it waits for that kernel (grid_dep_wait) before its
+// first dependent read. Hides the launch gap between dependent kernels.
+template <class... KArgs, class... Args>
+void launch_chained(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = grid;
+    lc.blockDim = block;
+    lc.dynamicSmemBytes = smem;
+    lc.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    AQ_CUDA(cudaLaunchKernelEx(&lc, k, args...));
+}
+#endif
+
 // Device buffer owned by a context; size in bytes.
 struct DevBuf {
     void* ptr = nullptr;
@@ -263,11 +284,11 @@ void nrc_train_step_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, const flo
 void nrc_encode_dev(aqua_ctx* ctx, NrcNet& net, const float* raw, int n, uint16_t* X);
 // tcgen05 inference (nrc_tc.cu)
 size_t nrc_tc_weight_bytes();
-void nrc_pack_tc(aqua_ctx* ctx, const float* w, void* img);
+// All three tcgen05 weight images: forward of w and of inf, backward of w.
+void nrc_pack_tc(aqua_ctx* ctx, const float* w, const float* inf, void* img_w, void* img_inf, void* img_bwd);
 void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n, float* out, uint32_t* err,
-                        uint32_t* acts = nullptr);
+                        uint32_t* acts = nullptr, double* loss_zero = nullptr);
 size_t nrc_tc_bwd_bytes();
-void nrc_pack_bwd_tc(aqua_ctx* ctx, const float* w, void* img);
 void nrc_backward_tc_dev(aqua_ctx* ctx, const void* img, const float* Y, const float* T, int n, float inv_count,
                          const uint32_t* acts, uint32_t* deltas, uint32_t* d6, double* loss, uint32_t* err);
 // Weight gradients of one training batch on tcgen05: per-chunk partials

@@ -313,10 +313,16 @@ __global__ void __launch_bounds__(128) k_nrc_wgrad(const uint32_t* __restrict__ 
 // ---------------------------------------------------------------- Adam
 // Kingma & Ba 2015. The gradient of parameter p is the sum of the chunk
 // partials in chunk order (deterministic).
+// With img_w non-null the new weights also go straight into the tcgen05
+// weight images (forward images of w and of the inference weights, backward
+// image of w), so no packing launch follows the step.
 __global__ void k_nrc_adam(const float* __restrict__ partial, int chunks, float* __restrict__ w,
                            float* __restrict__ m, float* __restrict__ v, float* __restrict__ grad, float lr,
                            float b1, float b2, float eps, float c1, float c2, float* __restrict__ ema,
-                           float ema_decay) {
+                           float ema_decay, uint8_t* __restrict__ img_w, uint8_t* __restrict__ img_inf,
+                           uint8_t* __restrict__ img_bwd) {
+    grid_dep_wait();
+    grid_dep_launch();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= kNrcParams) return;
     float g = 0.0f;
@@ -329,7 +335,20 @@ __global__ void k_nrc_adam(const float* __restrict__ partial, int chunks, float*
     float wn = w[p] - lr * (mm / c1) / (sqrtf(vv / c2) + eps);
     w[p] = wn;
     // Inference weights: exponential moving average of the trained ones.
-    if (ema_decay > 0.0f) ema[p] = ema_decay * ema[p] + (1.0f - ema_decay) * wn;
+    float inf = wn;
+    if (ema_decay > 0.0f) {
+        inf = ema_decay * ema[p] + (1.0f - ema_decay) * wn;
+        ema[p] = inf;
+    }
+    if (img_w) {
+        uint32_t fwd;
+        int32_t bwd;
+        nrc_tc_param_offsets(p, fwd, bwd);
+        const __nv_bfloat16 b = __float2bfloat16_rn(wn);
+        *reinterpret_cast<__nv_bfloat16*>(img_w + fwd) = b;
+        *reinterpret_cast<__nv_bfloat16*>(img_inf + fwd) = __float2bfloat16_rn(inf);
+        if (bwd >= 0) *reinterpret_cast<__nv_bfloat16*>(img_bwd + bwd) = b;
+    }
 }
 
 // ---------------------------------------------------------------- encoding
@@ -349,6 +368,8 @@ __global__ void __launch_bounds__(kEncRows) k_nrc_encode(const float* __restrict
     __shared__ float s_raw[kEncRows][kNrcRaw + 1];  // +1: conflict-free row reads
     __shared__ uint32_t s_out[kEncRows][33];
     const int t = threadIdx.x;
+    grid_dep_wait();
+    grid_dep_launch();
     const size_t row0 = (size_t)blockIdx.x * kEncRows;
     const int rows = min(kEncRows, n - (int)row0);
     const float* src = raw + row0 * kNrcRaw;
@@ -431,18 +452,20 @@ void nrc_init_weights(aqua_ctx* ctx, NrcNet& net, uint64_t seed) {
     nrc_set_weights(ctx, net, w.data());
 }
 
-void nrc_pack(aqua_ctx* ctx, NrcNet& net) {
+// mma.sync fragments of w (forward and backward) and of the inference
+// weights (the EMA when enabled).
+static void nrc_pack_frags(aqua_ctx* ctx, NrcNet& net) {
     int total = kFragFwd + kFragBwd;
     k_nrc_pack<<<(total + 255) / 256, 256, 0, ctx->stream>>>(net.w, net.frag, net.fragT);
-    // Forward fragments of the inference weights (the EMA when enabled).
     const float* inf = net.ema_decay > 0.0f ? net.ema : net.w;
     k_nrc_pack<<<(kFragFwd + 255) / 256, 256, 0, ctx->stream>>>(inf, net.frag_inf, nullptr);
     AQ_CUDA(cudaGetLastError());
-    if (net.forward_tc) {
-        nrc_pack_tc(ctx, inf, net.img_tc);
-        nrc_pack_tc(ctx, net.w, net.img_tc_w);
-        nrc_pack_bwd_tc(ctx, net.w, net.img_tc_bwd);
-    }
+}
+
+void nrc_pack(aqua_ctx* ctx, NrcNet& net) {
+    nrc_pack_frags(ctx, net);
+    if (net.forward_tc)
+        nrc_pack_tc(ctx, net.w, net.ema_decay > 0.0f ? net.ema : net.w, net.img_tc_w, net.img_tc, net.img_tc_bwd);
 }
 
 void nrc_set_weights(aqua_ctx* ctx, NrcNet& net, const float* host_w) {
@@ -498,11 +521,15 @@ void nrc_train_step_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, const flo
     cudaStream_t st = ctx->stream;
     const uint32_t* Xw = reinterpret_cast<const uint32_t*>(X);
     int g = nrc_grid(ctx, n);
-    if (net.forward_tc)
-        nrc_forward_tc_dev(ctx, net.img_tc_w, X, n, net.ty, net.tc_err, net.acts);
-    else
+    // On tcgen05 the four launches of a step (and of consecutive steps) are
+    // chained (programmatic dependent launch); the forward pass zeroes the
+    // loss word and Adam writes the next step's weight images.
+    if (net.forward_tc) {
+        nrc_forward_tc_dev(ctx, net.img_tc_w, X, n, net.ty, net.tc_err, net.acts, net.loss);
+    } else {
         k_nrc_forward<true><<<g, 128, 0, st>>>(Xw, n, net.frag, net.ty, net.acts);
-    AQ_CUDA(cudaMemsetAsync(net.loss, 0, 8, st));
+        AQ_CUDA(cudaMemsetAsync(net.loss, 0, 8, st));
+    }
     if (net.forward_tc)
         nrc_backward_tc_dev(ctx, net.img_tc_bwd, net.ty, target, n, 1.0f / (float)(n * kNrcOut), net.acts,
                             net.deltas, net.d6, net.loss, net.tc_err);
@@ -518,12 +545,12 @@ void nrc_train_step_dev(aqua_ctx* ctx, NrcNet& net, const uint16_t* X, const flo
     }
     net.step++;
     float c1 = 1.0f - powf(net.beta1, (float)net.step), c2 = 1.0f - powf(net.beta2, (float)net.step);
-    k_nrc_adam<<<(kNrcParams + 255) / 256, 256, 0, st>>>(net.partial, chunks, net.w, net.m, net.v, net.grad, net.lr,
-                                                         net.beta1, net.beta2, net.eps, c1, c2, net.ema,
-                                                         net.ema_decay);
-    nrc_pack(ctx, net);
+    launch_chained(k_nrc_adam, dim3((kNrcParams + 255) / 256), dim3(256), 0, st, (const float*)net.partial, chunks,
+                   net.w, net.m, net.v, net.grad, net.lr, net.beta1, net.beta2, net.eps, c1, c2, net.ema,
+                   net.ema_decay, net.forward_tc ? net.img_tc_w : nullptr, net.img_tc, net.img_tc_bwd);
+    if (!net.forward_tc) nrc_pack_frags(ctx, net);
     AQ_CUDA(cudaGetLastError());
-    net.launches += 5;
+    net.launches += net.forward_tc ? 4 : 6;
 }
 
 void nrc_check_tc(aqua_ctx* ctx, NrcNet& net) {
@@ -541,7 +568,8 @@ void nrc_encode_dev(aqua_ctx* ctx, NrcNet& net, const float* raw, int n, uint16_
     if (n <= 0) return;
     float3 bmin = make_float3(net.bmin[0], net.bmin[1], net.bmin[2]);
     float3 binv = make_float3(1.0f / net.bext[0], 1.0f / net.bext[1], 1.0f / net.bext[2]);
-    k_nrc_encode<<<(n + kEncRows - 1) / kEncRows, kEncRows, 0, ctx->stream>>>(raw, n, bmin, binv, X);
+    launch_chained(k_nrc_encode, dim3((n + kEncRows - 1) / kEncRows), dim3(kEncRows), 0, ctx->stream, raw, n, bmin,
+                   binv, X);
     AQ_CUDA(cudaGetLastError());
 }
 

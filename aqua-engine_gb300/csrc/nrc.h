@@ -37,6 +37,34 @@ constexpr int kNrcOut = 3;
 constexpr int kNrcParams = kNrcHiddenLayers * kNrcHidden * kNrcIn + kNrcOut * kNrcHidden;  // 20672
 constexpr int kNrcRaw = 16;  // raw vertex features, floats
 
+// Tensor-core weight images, bf16 in the no-swizzle K-major operand layout
+// (element (r, k) of an R-row tile at (k / 8) R 16 + r 16 + (k % 8) 2 bytes).
+// Forward image: W1..W5 as 64-row tiles (rows = outputs, K = inputs), then
+// W6 padded to 16 rows. Backward image: W6^T (64 rows = inputs, K = 16
+// outputs, 3 used), then W5^T..W2^T. Padding stays zero.
+constexpr int kNrcTcLayerBytes = 64 * 64 * 2;  // 8 KB
+constexpr int kNrcTcOutRows = 16;
+constexpr int kNrcTcBwdW6Bytes = 64 * 16 * 2;  // 2 KB
+
+AQ_HD constexpr uint32_t nrc_tc_offset(int rows, int r, int k) {
+    return (uint32_t)((k >> 3) * rows * 16 + r * 16 + (k & 7) * 2);
+}
+
+// Byte offsets of parameter p (row-major [out][in] per layer) in the forward
+// image and in the backward image; bwd = -1 for W1, which it leaves out.
+AQ_HD void nrc_tc_param_offsets(int p, uint32_t& fwd, int32_t& bwd) {
+    const int hidden = kNrcHiddenLayers * kNrcHidden * kNrcIn;
+    if (p < hidden) {
+        const int l = p / 4096, o = (p / 64) % 64, i = p % 64;
+        fwd = (uint32_t)(l * kNrcTcLayerBytes) + nrc_tc_offset(64, o, i);
+        bwd = l == 0 ? -1 : (int32_t)(kNrcTcBwdW6Bytes + (4 - l) * kNrcTcLayerBytes + nrc_tc_offset(64, i, o));
+    } else {
+        const int j = p - hidden, o = j / 64, i = j % 64;
+        fwd = (uint32_t)(5 * kNrcTcLayerBytes) + nrc_tc_offset(kNrcTcOutRows, o, i);
+        bwd = (int32_t)nrc_tc_offset(64, i, o);
+    }
+}
+
 // Raw vertex features, 16 floats: position (3), outgoing direction (3),
 // normal (3), roughness (1), diffuse albedo (3), specular F0 (3).
 struct NrcRaw {

@@ -45,8 +45,8 @@ constexpr int kTcRows = 128;                      // rows per tile (MMA M)
 constexpr int kTcGroups = 4;                      // warpgroups (tiles in flight) per CTA, training kernels
 constexpr int kTcThreads = 128 * kTcGroups;
 constexpr int kTcTileBytes = kTcRows * 64 * 2;    // 16 KB per input or activation tile
-constexpr int kTcLayerBytes = 64 * 64 * 2;        // 8 KB hidden-layer weights
-constexpr int kTcOutRows = 16;                    // output layer padded to N = 16 (3 used)
+constexpr int kTcLayerBytes = kNrcTcLayerBytes;  // 8 KB hidden-layer weights
+constexpr int kTcOutRows = kNrcTcOutRows;        // output layer padded to N = 16 (3 used)
 constexpr int kTcOutBytes = kTcOutRows * 64 * 2;  // 2 KB
 constexpr int kTcWeightBytes = 5 * kTcLayerBytes + kTcOutBytes;  // 42 KB
 constexpr uint32_t kTcGroupCols = 128;            // accumulator 64 + activations 32, rounded up
@@ -67,24 +67,22 @@ static_assert((kTcTmemCols & (kTcTmemCols - 1)) == 0 && kTcTmemCols >= 32 && kTc
 static_assert(kTcWeightBytes % 1024 == 0 && kTcTileBytes % 1024 == 0, "tiles stay 1024-byte aligned");
 
 // Byte offset of element (r, k) in an R-row operand tile.
-__host__ __device__ constexpr uint32_t tc_offset(int rows, int r, int k) {
-    return (uint32_t)((k >> 3) * rows * 16 + r * 16 + (k & 7) * 2);
-}
+__host__ __device__ constexpr uint32_t tc_offset(int rows, int r, int k) { return nrc_tc_offset(rows, r, k); }
 
-// Weights (rows = outputs, K = inputs) into the operand layout, bf16:
-// W1..W5 (64 rows each) then W6 padded to 16 rows.
-__global__ void k_nrc_pack_tc(const float* __restrict__ w, uint8_t* __restrict__ img) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;  // one element
-    const int hidden = 5 * 64 * 64;
-    if (i < hidden) {
-        int l = i / 4096, r = (i / 64) % 64, k = i % 64;
-        *reinterpret_cast<__nv_bfloat16*>(img + l * kTcLayerBytes + tc_offset(64, r, k)) = __float2bfloat16_rn(w[i]);
-    } else if (i < hidden + kTcOutRows * 64) {
-        int j = i - hidden, r = j / 64, k = j % 64;
-        float x = r < kNrcOut ? w[hidden + r * 64 + k] : 0.0f;
-        *reinterpret_cast<__nv_bfloat16*>(img + 5 * kTcLayerBytes + tc_offset(kTcOutRows, r, k)) =
-            __float2bfloat16_rn(x);
-    }
+// All three weight images from the FP32 weights w and the inference
+// weights inf (nrc_tc_param_offsets; the caller zeroes the padding first):
+// forward images of w (training) and of inf (inference), backward image of w.
+__global__ void k_nrc_pack_tc(const float* __restrict__ w, const float* __restrict__ inf, uint8_t* __restrict__ img_w,
+                              uint8_t* __restrict__ img_inf, uint8_t* __restrict__ img_bwd) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;  // one parameter
+    if (p >= kNrcParams) return;
+    uint32_t fwd;
+    int32_t bwd;
+    nrc_tc_param_offsets(p, fwd, bwd);
+    const __nv_bfloat16 b = __float2bfloat16_rn(w[p]);
+    *reinterpret_cast<__nv_bfloat16*>(img_w + fwd) = b;
+    *reinterpret_cast<__nv_bfloat16*>(img_inf + fwd) = __float2bfloat16_rn(inf[p]);
+    if (bwd >= 0) *reinterpret_cast<__nv_bfloat16*>(img_bwd + bwd) = b;
 }
 
 // ---------------------------------------------------------------- PTX wrappers
@@ -220,7 +218,8 @@ __device__ __forceinline__ uint32_t relu_pack2(uint32_t lo, uint32_t hi) {
 // as bf16 rows, acts[l][row][64], for the backward pass.
 __global__ void __launch_bounds__(kTcFwdThreads, 1)
     k_nrc_forward_tc(const __grid_constant__ CUtensorMap xmap, int n, const uint4* __restrict__ wimg,
-                     float* __restrict__ out, uint32_t* __restrict__ err, uint4* __restrict__ acts) {
+                     float* __restrict__ out, uint32_t* __restrict__ err, uint4* __restrict__ acts,
+                     double* __restrict__ loss_zero) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t bar_in[kTcFwdGroups], bar_mma[kTcFwdGroups];
     __shared__ uint32_t tmem_base_slot;
@@ -232,6 +231,9 @@ __global__ void __launch_bounds__(kTcFwdThreads, 1)
     const uint32_t sW = base;
     const uint32_t sI = base + kTcWeightBytes + (uint32_t)g * kTcTileBytes;  // this group's input tile
 
+    grid_dep_wait();  // the weights and inputs come from the kernels before
+    grid_dep_launch();
+    if (loss_zero && blockIdx.x == 0 && tid == 0) *loss_zero = 0.0;  // the training step's loss word
     for (int i = tid; i < kTcWeightBytes / 16; i += kTcFwdThreads) reinterpret_cast<uint4*>(sbase)[i] = wimg[i];
     if (tid < kTcFwdGroups) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar_in[tid])) : "memory");
@@ -381,25 +383,10 @@ __global__ void __launch_bounds__(kTcFwdThreads, 1)
 // 1, stores it back to TMEM as the A operand of dH_{l-1} = delta_l x W_l.
 // Weight image (rows = N = 64 inputs, K = outputs): W6^T (K = 16) then
 // W5^T..W2^T (K = 64).
-constexpr int kTcBwdW6Bytes = 64 * 16 * 2;                         // 2 KB
+constexpr int kTcBwdW6Bytes = kNrcTcBwdW6Bytes;                    // 2 KB
 constexpr int kTcBwdBytes = kTcBwdW6Bytes + 4 * kTcLayerBytes;      // 34 KB
 constexpr int kTcBwdSmemBytes = std::max(kTcBwdBytes + 1024, 120 * 1024);  // one CTA per SM
 constexpr float kTcLossEps = 0.01f;
-
-__global__ void k_nrc_pack_bwd_tc(const float* __restrict__ w, uint8_t* __restrict__ img) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < 64 * 16) {  // W6^T: row r = input, k = output (3 used)
-        int r = i / 16, k = i % 16;
-        float x = k < kNrcOut ? w[5 * 4096 + k * 64 + r] : 0.0f;
-        *reinterpret_cast<__nv_bfloat16*>(img + tc_offset(64, r, k)) = __float2bfloat16_rn(x);
-    } else if (i < 64 * 16 + 4 * 4096) {  // W5^T, W4^T, W3^T, W2^T
-        int j = i - 64 * 16, m = j / 4096, r = (j / 64) % 64, k = j % 64;
-        int layer = 4 - m;  // W5 = layer index 4 of the stored weights
-        float x = w[layer * 4096 + k * 64 + r];
-        *reinterpret_cast<__nv_bfloat16*>(img + kTcBwdW6Bytes + m * kTcLayerBytes + tc_offset(64, r, k)) =
-            __float2bfloat16_rn(x);
-    }
-}
 
 __device__ __forceinline__ uint32_t pack2_rn(float lo, float hi) {
     uint32_t d;
@@ -426,6 +413,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int g = warp >> 2, q = warp & 3, gt = tid & 127;
     const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
     uint8_t* sbase = smem_raw + (base - smem_u32(smem_raw));
+    grid_dep_wait();
+    grid_dep_launch();
     for (int i = tid; i < kTcBwdBytes / 16; i += kTcThreads) reinterpret_cast<uint4*>(sbase)[i] = wimg[i];
     if (tid < kTcGroups)
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar_mma[tid])) : "memory");
@@ -558,9 +547,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 // ---------------------------------------------------------------- host side
 size_t nrc_tc_weight_bytes() { return (size_t)kTcWeightBytes; }
 
-void nrc_pack_tc(aqua_ctx* ctx, const float* w, void* img) {
-    int total = 5 * 4096 + kTcOutRows * 64;
-    k_nrc_pack_tc<<<(total + 255) / 256, 256, 0, ctx->stream>>>(w, (uint8_t*)img);
+void nrc_pack_tc(aqua_ctx* ctx, const float* w, const float* inf, void* img_w, void* img_inf, void* img_bwd) {
+    AQ_CUDA(cudaMemsetAsync(img_w, 0, kTcWeightBytes, ctx->stream));
+    AQ_CUDA(cudaMemsetAsync(img_inf, 0, kTcWeightBytes, ctx->stream));
+    AQ_CUDA(cudaMemsetAsync(img_bwd, 0, kTcBwdBytes, ctx->stream));
+    k_nrc_pack_tc<<<(kNrcParams + 255) / 256, 256, 0, ctx->stream>>>(w, inf, (uint8_t*)img_w, (uint8_t*)img_inf,
+                                                                     (uint8_t*)img_bwd);
     AQ_CUDA(cudaGetLastError());
 }
 
@@ -581,7 +573,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n, float* out, uint32_t* err,
-                        uint32_t* acts) {
+                        uint32_t* acts, double* loss_zero) {
     if (n <= 0) return;
     if (((uintptr_t)X & 15) != 0) throw Error(AQUA_ERR_INVALID_ARG, "x must be 16-byte aligned");
     CUtensorMap map;
@@ -599,8 +591,8 @@ void nrc_forward_tc_dev(aqua_ctx* ctx, const void* img, const uint16_t* X, int n
     }
     const int tiles = (n + kTcRows - 1) / kTcRows;
     const int grid = std::max(1, std::min(tiles, ctx->num_sms));
-    k_nrc_forward_tc<<<grid, kTcFwdThreads, kTcFwdSmemBytes, ctx->stream>>>(map, n, reinterpret_cast<const uint4*>(img),
-                                                                       out, err, reinterpret_cast<uint4*>(acts));
+    launch_chained(k_nrc_forward_tc, dim3(grid), dim3(kTcFwdThreads), kTcFwdSmemBytes, ctx->stream, map, n,
+                   reinterpret_cast<const uint4*>(img), out, err, reinterpret_cast<uint4*>(acts), loss_zero);
     AQ_CUDA(cudaGetLastError());
 }
 
@@ -667,6 +659,8 @@ __global__ void __launch_bounds__(kWgTcThreads, 2) k_nrc_wgrad_tc(const uint16_t
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
+    grid_dep_wait();  // the activations and deltas come from the kernels before
+    grid_dep_launch();
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
                      "r"(64u)
@@ -802,20 +796,14 @@ int nrc_wgrad_tc_dev(aqua_ctx* ctx, const uint16_t* X, const uint32_t* acts, con
     }
     const int rows = wgrad_chunk_rows(n);
     const int chunks = (n + rows - 1) / rows;
-    k_nrc_wgrad_tc<<<dim3(chunks, 6), kWgTcThreads, kWgTcSmem, ctx->stream>>>(
-        X, reinterpret_cast<const uint16_t*>(acts), reinterpret_cast<const uint16_t*>(deltas),
-        reinterpret_cast<const uint16_t*>(d6), n, rows, partial, err);
+    launch_chained(k_nrc_wgrad_tc, dim3(chunks, 6), dim3(kWgTcThreads), kWgTcSmem, ctx->stream, X,
+                   reinterpret_cast<const uint16_t*>(acts), reinterpret_cast<const uint16_t*>(deltas),
+                   reinterpret_cast<const uint16_t*>(d6), n, rows, partial, err);
     AQ_CUDA(cudaGetLastError());
     return chunks;
 }
 
 size_t nrc_tc_bwd_bytes() { return (size_t)kTcBwdBytes; }
-
-void nrc_pack_bwd_tc(aqua_ctx* ctx, const float* w, void* img) {
-    int total = 64 * 16 + 4 * 4096;
-    k_nrc_pack_bwd_tc<<<(total + 255) / 256, 256, 0, ctx->stream>>>(w, (uint8_t*)img);
-    AQ_CUDA(cudaGetLastError());
-}
 
 void nrc_backward_tc_dev(aqua_ctx* ctx, const void* img, const float* Y, const float* T, int n, float inv_count,
                          const uint32_t* acts, uint32_t* deltas, uint32_t* d6, double* loss, uint32_t* err) {
@@ -827,9 +815,9 @@ void nrc_backward_tc_dev(aqua_ctx* ctx, const void* img, const float* Y, const f
     }
     const int tiles = (n + kTcRows - 1) / kTcRows;
     const int grid = std::max(1, std::min(tiles, ctx->num_sms));
-    k_nrc_backward_tc<<<grid, kTcThreads, kTcBwdSmemBytes, ctx->stream>>>(
-        Y, T, n, inv_count, reinterpret_cast<const uint4*>(img), reinterpret_cast<const uint4*>(acts),
-        reinterpret_cast<uint4*>(deltas), reinterpret_cast<uint4*>(d6), loss, err);
+    launch_chained(k_nrc_backward_tc, dim3(grid), dim3(kTcThreads), kTcBwdSmemBytes, ctx->stream, Y, T, n,
+                   inv_count, reinterpret_cast<const uint4*>(img), reinterpret_cast<const uint4*>(acts),
+                   reinterpret_cast<uint4*>(deltas), reinterpret_cast<uint4*>(d6), loss, err);
     AQ_CUDA(cudaGetLastError());
 }
 

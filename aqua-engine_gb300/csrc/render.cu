@@ -682,25 +682,6 @@ void workspace_release(aqua_ctx* ctx) {
     ctx->ws = Workspace{};
 }
 
-// Launches kernel k chained to the previous work in stream st (programmatic
-// dependent launch): its blocks may be scheduled while the previous kernel's
-// last blocks drain, and it waits for that kernel (grid_dep_wait) before its
-// first dependent read. Hides the launch gap between the wavefront stages.
-template <class... KArgs, class... Args>
-static void launch_chained(void (*k)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
-    cudaLaunchConfig_t lc = {};
-    lc.gridDim = dim3((unsigned)grid);
-    lc.blockDim = dim3((unsigned)block);
-    lc.dynamicSmemBytes = 0;
-    lc.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    lc.attrs = attr;
-    lc.numAttrs = 1;
-    AQ_CUDA(cudaLaunchKernelEx(&lc, k, args...));
-}
-
 template <class K>
 static int grid_for(aqua_ctx* ctx, K kernel, int block, int blocks_per_sm) {
     int per_sm = blocks_per_sm;
@@ -878,11 +859,11 @@ void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, 
             // the events barely perturb the launch stream.
             bool timed = timing && (iter % kStageTimingStride) == 0;
             if (timed) tt.begin();
-            launch_chained(trace_k, g_trace, bt, st, S, P, W, in, out);
+            launch_chained(trace_k, g_trace, bt, 0, st, S, P, W, in, out);
             if (timed) { tt.end(); ts.begin(); }
-            launch_chained(shade_k, g_shade, bs, st, S, P, W, in, out);
+            launch_chained(shade_k, g_shade, bs, 0, st, S, P, W, in, out);
             if (timed) { ts.end(); tsh.begin(); }
-            launch_chained(shadow_k, g_shadow, bt, st, S, P, W);
+            launch_chained(shadow_k, g_shadow, bt, 0, st, S, P, W);
             if (timed) tsh.end();
             launches += 3;
         }
@@ -949,6 +930,8 @@ void render_path(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, 
 // samples of one pixel may have queried, so the add is atomic.
 __global__ void k_nrc_resolve(const float4* __restrict__ q_pix, const float* __restrict__ pred, uint32_t n,
                               float4* film) {
+    grid_dep_wait();
+    grid_dep_launch();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 q = q_pix[i];
         uint32_t pixel = (uint32_t)__float_as_int(q.x);
@@ -970,6 +953,8 @@ constexpr float kNrcMaxTarget = 1e3f;
 __global__ void k_nrc_targets(const float4* __restrict__ rec, uint32_t n, const float4* __restrict__ ltrain,
                               const float4* __restrict__ lsnap, int train_span, int train_depth, uint64_t a,
                               uint64_t b, float* __restrict__ raw_out, float* __restrict__ t_out) {
+    grid_dep_wait();
+    grid_dep_launch();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4* r = rec + 6 * (size_t)i;
         uint32_t j = (uint32_t)((a * (uint64_t)i + b) % (uint64_t)n);
@@ -1138,9 +1123,9 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
             uint32_t in = (uint32_t)(iter & 1), out = 1u - in;
             W.q_in = w.q[in];
             W.q_out = w.q[out];
-            launch_chained(trace_k, g_trace, 128, st, S, P, W, in, out);
-            launch_chained(shade_k, g_shade, 128, st, S, P, W, in, out);
-            launch_chained(shadow_k, g_shadow, 128, st, S, P, W);
+            launch_chained(trace_k, g_trace, 128, 0, st, S, P, W, in, out);
+            launch_chained(shade_k, g_shade, 128, 0, st, S, P, W, in, out);
+            launch_chained(shadow_k, g_shadow, 128, 0, st, S, P, W);
             launches += 3;
         }
         AQ_CUDA(cudaGetLastError());
@@ -1157,7 +1142,8 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
         nrc_encode_dev(ctx, net, nw.q_raw, (int)nq, nw.q_x);
         nrc_forward_dev(ctx, net, nw.q_x, (int)nq, nw.q_pred);
         int g = (int)std::min<size_t>((nq + 255) / 256, (size_t)ctx->num_sms * 16);
-        k_nrc_resolve<<<g, 256, 0, st>>>(nw.q_pix, nw.q_pred, nq, w.film);
+        launch_chained(k_nrc_resolve, dim3(g), dim3(256), 0, st, (const float4*)nw.q_pix, (const float*)nw.q_pred, nq,
+                       w.film);
         AQ_CUDA(cudaGetLastError());
         launches += 3;
     }
@@ -1171,7 +1157,7 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
         while (gcd64(a, nrec) != 1) ++a;
         int g = (int)std::min<size_t>((nrec + 255) / 256, (size_t)ctx->num_sms * 16);
         k_nrc_targets<<<g, 256, 0, st>>>(nw.rec, nrec, nw.ltrain, nw.lsnap, train_span, train_depth, a, b, nw.t_raw,
-                                          nw.t_target);
+                                          nw.t_target);  // after an event record: nothing to chain to
         AQ_CUDA(cudaGetLastError());
         nrc_encode_dev(ctx, net, nw.t_raw, (int)nrec, nw.t_x);
         launches += 2;
@@ -1182,7 +1168,7 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
             size_t r0 = (size_t)sidx * (size_t)batch;
             int rows = (int)std::min<size_t>((size_t)batch, nrec - r0);
             nrc_train_step_dev(ctx, net, nw.t_x + 64 * r0, nw.t_target + 3 * r0, rows);
-            launches += 5;
+            launches += net.forward_tc ? 4 : 6;
         }
         AQ_CUDA(cudaMemcpyAsync(&loss, net.loss, 8, cudaMemcpyDeviceToHost, st));
         // Aim the next frame's training-path fraction at the record budget.
