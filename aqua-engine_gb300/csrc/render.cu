@@ -1346,9 +1346,9 @@ void render_noalloc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cf
             uint32_t in = (uint32_t)(iter & 1), out = 1u - in;
             W.q_in = q[in];
             W.q_out = q[out];
-            trace_k<<<g_trace, 128, 0, st>>>(S, P, W, in, out);
-            shade_k<<<g_shade, 128, 0, st>>>(S, P, W, in, out);
-            shadow_k<<<g_shadow, 128, 0, st>>>(S, P, W);
+            launch_chained(trace_k, g_trace, 128, 0, st, S, P, W, in, out);
+            launch_chained(shade_k, g_shade, 128, 0, st, S, P, W, in, out);
+            launch_chained(shadow_k, g_shadow, 128, 0, st, S, P, W);
             launches += 3;
         }
         AQ_CUDA(cudaGetLastError());
