@@ -266,6 +266,22 @@ def test_stats_and_stage_timing(gpu_ctx):
     s.free()
 
 
+def test_chained_launches_match_event_separated_ones(gpu_ctx):
+    """The wavefront stages are chained by programmatic dependent launch;
+    stage timing records events between the launches of every 8th iteration,
+    which separates those launches. The image is the same bit for bit."""
+    import aqua
+
+    s = gpu_ctx.procedural(2, seed=0, width=256, height=256)
+    cfg = gpu_ctx.integrator(spp=64, max_depth=8, rr_depth=3, seed=4)
+    tune = gpu_ctx.tuning(replicas=1)
+    chained, st = gpu_ctx.render(s, cfg, tuning=tune)
+    timed, st2 = gpu_ctx.render(s, cfg, tuning=tune, flags=aqua.RENDER_STAGE_TIMING)
+    assert st.iterations > 100 and st2.iterations == st.iterations
+    assert np.array_equal(chained.view(np.uint32), timed.view(np.uint32))
+    s.free()
+
+
 def test_allocation_failure_is_reported():
     import aqua
 
