@@ -74,7 +74,12 @@ __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.w
 __device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
 
 // Two consecutive 16-byte words in one 256-bit load through the read-only
-// path (sm_100 and later); p must be 32-byte aligned.
+// (non-coherent) path (sm_100 and later); p must be 32-byte aligned. Only
+// for data that nothing writes during the render (scene nodes): kernels
+// chained by programmatic dependent launch may begin before their
+// predecessor has finished, and the non-coherent path is outside what
+// griddepcontrol.wait makes visible, so they read what earlier kernels of
+// the chain wrote through coherent loads (plain or __ldcg).
 __device__ __forceinline__ void ldg2x4(const float4* p, float4& a, float4& b) {
     asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
         : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)

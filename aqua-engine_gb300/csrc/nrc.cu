@@ -326,7 +326,7 @@ __global__ void k_nrc_adam(const float* __restrict__ partial, int chunks, float*
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= kNrcParams) return;
     float g = 0.0f;
-    for (int k = 0; k < chunks; ++k) g += partial[(size_t)k * kNrcParams + p];
+    for (int k = 0; k < chunks; ++k) g += __ldcg(partial + (size_t)k * kNrcParams + p);
     grad[p] = g;
     float mm = b1 * m[p] + (1.0f - b1) * g;
     float vv = b2 * v[p] + (1.0f - b2) * g * g;
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(kEncRows) k_nrc_encode(const float* __restrict
     const size_t row0 = (size_t)blockIdx.x * kEncRows;
     const int rows = min(kEncRows, n - (int)row0);
     const float* src = raw + row0 * kNrcRaw;
-    for (int k = t; k < rows * kNrcRaw; k += kEncRows) s_raw[k / kNrcRaw][k % kNrcRaw] = src[k];
+    for (int k = t; k < rows * kNrcRaw; k += kEncRows) s_raw[k / kNrcRaw][k % kNrcRaw] = __ldcg(src + k);
     __syncthreads();
     if (t < rows) {
         const float* r = s_raw[t];

@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(kTcFwdThreads, 1)
     grid_dep_wait();  // the weights and inputs come from the kernels before
     grid_dep_launch();
     if (loss_zero && blockIdx.x == 0 && tid == 0) *loss_zero = 0.0;  // the training step's loss word
-    for (int i = tid; i < kTcWeightBytes / 16; i += kTcFwdThreads) reinterpret_cast<uint4*>(sbase)[i] = wimg[i];
+    for (int i = tid; i < kTcWeightBytes / 16; i += kTcFwdThreads) reinterpret_cast<uint4*>(sbase)[i] = __ldcg(wimg + i);
     if (tid < kTcFwdGroups) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar_in[tid])) : "memory");
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar_mma[tid])) : "memory");
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint8_t* sbase = smem_raw + (base - smem_u32(smem_raw));
     grid_dep_wait();
     grid_dep_launch();
-    for (int i = tid; i < kTcBwdBytes / 16; i += kTcThreads) reinterpret_cast<uint4*>(sbase)[i] = wimg[i];
+    for (int i = tid; i < kTcBwdBytes / 16; i += kTcThreads) reinterpret_cast<uint4*>(sbase)[i] = __ldcg(wimg + i);
     if (tid < kTcGroups)
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar_mma[tid])) : "memory");
     if (tid == 0) asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -448,7 +448,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (valid) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                float y = Y[(size_t)grow * 3 + c], t = T[(size_t)grow * 3 + c];
+                float y = __ldcg(Y + (size_t)grow * 3 + c), t = __ldcg(T + (size_t)grow * 3 + c);
                 float den = y * y + kTcLossEps, d = y - t;
                 lsum += d * d / den;
                 gy[c] = 2.0f * d / den * inv_count;
@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 uint4 h[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j)
-                    h[j] = valid ? acts[((size_t)l * (size_t)n + (size_t)grow) * 8 + (size_t)j] : make_uint4(0, 0, 0, 0);
+                    h[j] = valid ? __ldcg(acts + ((size_t)l * (size_t)n + (size_t)grow) * 8 + (size_t)j) : make_uint4(0, 0, 0, 0);
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const uint32_t hw[4] = {h[j].x, h[j].y, h[j].z, h[j].w};
@@ -682,10 +682,10 @@ __global__ void __launch_bounds__(kWgTcThreads, 2) k_nrc_wgrad_tc(const uint16_t
 #pragma unroll
         for (int q = 0; q < kWgTcLoads; ++q) {
             const int idx = tid + kWgTcThreads * q, row = r0 + (idx >> 3);
-            rh[q] = row < n ? reinterpret_cast<const uint4*>(H + (size_t)row * 64)[idx & 7] : make_uint4(0, 0, 0, 0);
+            rh[q] = row < n ? __ldcg(reinterpret_cast<const uint4*>(H + (size_t)row * 64) + (idx & 7)) : make_uint4(0, 0, 0, 0);
             const int row_d = r0 + idx / dq;
             rd[q] = (idx < kWgTcSlice * dq && row_d < n)
-                        ? reinterpret_cast<const uint4*>(D + (size_t)row_d * dcols)[idx % dq]
+                        ? __ldcg(reinterpret_cast<const uint4*>(D + (size_t)row_d * dcols) + idx % dq)
                         : make_uint4(0, 0, 0, 0);
         }
     };

@@ -933,12 +933,12 @@ __global__ void k_nrc_resolve(const float4* __restrict__ q_pix, const float* __r
     grid_dep_wait();
     grid_dep_launch();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 q = q_pix[i];
+        float4 q = __ldcg(q_pix + i);
         uint32_t pixel = (uint32_t)__float_as_int(q.x);
         float* f = reinterpret_cast<float*>(film + pixel);
-        atomicAdd(f + 0, q.y * fmaxf(pred[3 * (size_t)i + 0], 0.0f));
-        atomicAdd(f + 1, q.z * fmaxf(pred[3 * (size_t)i + 1], 0.0f));
-        atomicAdd(f + 2, q.w * fmaxf(pred[3 * (size_t)i + 2], 0.0f));
+        atomicAdd(f + 0, q.y * fmaxf(__ldcg(pred + 3 * (size_t)i + 0), 0.0f));
+        atomicAdd(f + 1, q.z * fmaxf(__ldcg(pred + 3 * (size_t)i + 1), 0.0f));
+        atomicAdd(f + 2, q.w * fmaxf(__ldcg(pred + 3 * (size_t)i + 2), 0.0f));
     }
 }
 
