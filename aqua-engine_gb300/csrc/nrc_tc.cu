@@ -682,10 +682,10 @@ __global__ void __launch_bounds__(kWgTcThreads, 2) k_nrc_wgrad_tc(const uint16_t
 #pragma unroll
         for (int q = 0; q < kWgTcLoads; ++q) {
             const int idx = tid + kWgTcThreads * q, row = r0 + (idx >> 3);
-            rh[q] = row < n ? __ldcg(reinterpret_cast<const uint4*>(H + (size_t)row * 64) + (idx & 7)) : make_uint4(0, 0, 0, 0);
+            rh[q] = row < n ? __ldca(reinterpret_cast<const uint4*>(H + (size_t)row * 64) + (idx & 7)) : make_uint4(0, 0, 0, 0);
             const int row_d = r0 + idx / dq;
             rd[q] = (idx < kWgTcSlice * dq && row_d < n)
-                        ? __ldcg(reinterpret_cast<const uint4*>(D + (size_t)row_d * dcols) + idx % dq)
+                        ? __ldca(reinterpret_cast<const uint4*>(D + (size_t)row_d * dcols) + idx % dq)
                         : make_uint4(0, 0, 0, 0);
         }
     };
