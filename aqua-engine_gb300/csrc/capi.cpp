@@ -584,7 +584,7 @@ AQUA_API void aqua_tuning_defaults(aqua_tuning* t) {
     memset(t, 0, sizeof(*t));
     t->block_trace = 128;
     t->block_shade = 128;
-    t->sort_by_material = 1;
+    t->sort_by_material = 0;  // unsorted with deep queues beats the material sort (render.cu, plan_slots)
     t->iters_per_graph = 16;
 }
 

@@ -332,12 +332,33 @@ SPHERES_WORKLOAD = {"workload": "sphere-field-1024x1024-64spp-depth8", "width": 
 # DRAM bytes (read + write) of one full-queue k_trace_ext launch from ncu
 # captures of these scenes, and the rays that launch traced.
 TRACE_TRAFFIC = {
-    "interior": {"bytes": 564.4e6, "rays": 2073600,
-                 "source": "ncu capture of a full-queue launch inside a 1080p interior render "
-                           "(497.3 MB read + 67.1 MB written)"},
-    "spheres": {"bytes": 180.36e6, "rays": 1048576,
-                "source": "ncu capture of the sphere field (172.6 MB read + 7.7 MB written, the render's "
-                          "third launch: full queue of camera and first-bounce rays)"},
+    "cornell": {"bytes": 849.785e6, "rays": 16777216,
+                "source": "ncu capture of the first k_trace_ext launch of a 16-spp Cornell GGX 1024x1024 render at "
+                          "the default queue depth (16 replicas: 16,777,216 camera rays; 604.5 MB read + 245.3 MB "
+                          "written)"},
+    "interior": {"bytes": 1212.296e6, "rays": 16588800,
+                 "source": "ncu capture of the first k_trace_ext launch of a 16-spp 1080p interior render at the "
+                           "default queue depth (8 replicas: 16,588,800 camera rays; 918.3 MB read + 293.9 MB "
+                           "written; bounce-ray launches cost up to 1.4x more per ray)"},
+    "spheres": {"bytes": 1943.945e6, "rays": 16777216,
+                "source": "ncu capture of the first k_trace_ext launch of a 16-spp sphere-field render at the "
+                          "default queue depth (16 replicas: 16,777,216 camera rays; 1668.6 MB read + 275.4 MB "
+                          "written)"},
+}
+
+
+# Algorithmic bytes of k_shade: per shaded path it reads the queue entry
+# (4 B), path state and throughput (32), hit (16), direction (16), triangle
+# (48) and material (32) and writes the continued or restarted path (ray,
+# throughput, state: 64) and its next-queue entry (4); per next-event
+# estimate it writes a shadow record (48).
+SHADE_BYTES_PER_PATH = 4 + 32 + 16 + 16 + 48 + 32 + 64 + 4
+SHADOW_RECORD_BYTES = 48
+# DRAM bytes of one full-queue k_shade launch from an ncu capture.
+SHADE_TRAFFIC = {
+    "cornell": {"bytes": 2636.587e6, "paths": 16777216,
+                "source": "ncu capture of the first k_shade launch of a 16-spp Cornell GGX 1024x1024 render at the "
+                          "default queue depth (16,777,216 camera-ray hits; 1162.1 MB read + 1474.5 MB written)"},
 }
 
 
@@ -622,27 +643,54 @@ def run_gpu(args, world, rank, local, pg):
     all_paths = sum_over_ranks(pg, paths)
     value = all_paths / (ms_max * 1e-3) / 1e6
 
-    # Dominant kernel: closest-hit traversal. Its launch times come from one
-    # more render of the same step with CUDA events around every 8th
-    # iteration's launches (RENDER_STAGE_TIMING), run after the timed steps
-    # so the events do not stretch them.
+    # Rooflines of the two largest stages. Launch times come from one more
+    # render of the same step with CUDA events around every 8th iteration's
+    # launches (RENDER_STAGE_TIMING), run after the timed steps so the events
+    # do not stretch them; `roofline` is the stage with the larger sampled time.
     flush.zero_()
     torch.cuda.synchronize()
     staged = ctx.render_device(scene, cfg, film.data_ptr(), tune, flags=aqua.RENDER_STAGE_TIMING)
-    trace_ms = staged.trace_ms
-    launches = staged.trace_launches
+    iters = max(staged.iterations, 1)
+    rays_per_launch = staged.ext_rays / iters
+    # Closest-hit traversal (k_trace_ext).
     ext = cst.ext_rays
     bytes_step = cst.node_visits * NODE_BYTES + cst.tri_tests * 48 + ext * (32 + 16)
     bytes_per_launch = bytes_step / max(cst.trace_launches, 1)
-    avg_launch_s = trace_ms * 1e-3 / max(launches, 1)
+    avg_launch_s = staged.trace_ms * 1e-3 / max(staged.trace_launches, 1)
     achieved = bytes_per_launch / avg_launch_s / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": args.traffic_per_launch, "peak_source": peak_src,
-                "kernel": "k_trace_ext (closest-hit BVH traversal)",
-                "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6,
-                "note": f"algorithmic bytes = node visits x {NODE_BYTES} B (four-wide node: six box words and the "
-                        "child links) + triangle tests x 48 B + 48 B per ray; the Cornell BVH (8 nodes) is "
-                        "cache-resident, so DRAM traffic is far below this"}
+    if args.traffic_per_launch > 0:
+        traffic = args.traffic_per_launch
+    else:  # the ncu DRAM bytes per ray of a full-queue launch, scaled to this launch's mean ray count
+        tc = TRACE_TRAFFIC["cornell"]
+        traffic = tc["bytes"] / tc["rays"] * rays_per_launch
+    trace_roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                  "traffic": traffic, "rays_per_launch": rays_per_launch, "peak_source": peak_src,
+                  "traffic_note": "ncu DRAM bytes per ray of a full-queue launch scaled to this launch's mean ray "
+                                  "count; " + TRACE_TRAFFIC["cornell"]["source"],
+                  "kernel": "k_trace_ext (closest-hit BVH traversal)",
+                  "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6,
+                  "sampled_ms": staged.trace_ms,
+                  "note": f"algorithmic bytes = node visits x {NODE_BYTES} B (four-wide node: six box words and the "
+                          "child links) + triangle tests x 48 B + 48 B per ray; the Cornell BVH (8 nodes) is "
+                          "cache-resident (L1/L2), so the algorithmic rate can pass the HBM copy rate while DRAM "
+                          "traffic stays far below it"}
+    # Shading (k_shade).
+    sh_per_launch = staged.shadow_rays / iters
+    shade_bytes = rays_per_launch * SHADE_BYTES_PER_PATH + sh_per_launch * SHADOW_RECORD_BYTES
+    shade_s = staged.shade_ms * 1e-3 / max(staged.shade_launches, 1)
+    shade_gbs = shade_bytes / shade_s / 1e9
+    st_tr = SHADE_TRAFFIC.get("cornell")
+    shade_roof = {"bound": "hbm", "achieved": shade_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": shade_gbs / hbm_peak,
+                  "traffic": st_tr["bytes"] / st_tr["paths"] * rays_per_launch if st_tr else None,
+                  "traffic_note": "ncu DRAM bytes per path of a full-queue launch scaled to this launch's mean path "
+                                  "count; " + st_tr["source"] if st_tr else None,
+                  "paths_per_launch": rays_per_launch, "peak_source": peak_src,
+                  "kernel": "k_shade (emission, next-event estimation, BSDF sampling, roulette, path restart)",
+                  "bytes_per_launch": shade_bytes, "avg_launch_us": shade_s * 1e6, "sampled_ms": staged.shade_ms,
+                  "note": f"algorithmic bytes = {SHADE_BYTES_PER_PATH} B per shaded path (queue entry, path state, "
+                          "hit, direction, triangle, material read; path state and next-queue entry written) + "
+                          f"{SHADOW_RECORD_BYTES} B per shadow record written"}
+    roofline = shade_roof if staged.shade_ms >= staged.trace_ms else trace_roof
 
     # End to end through the C ABI with host buffers: scene upload from
     # pinned host memory + render + film download every step, over the same
@@ -663,8 +711,9 @@ def run_gpu(args, world, rank, local, pg):
     e2e_value = sum_over_ranks(pg, e2e_paths) / e2e_s / 1e6
 
     l2 = measure_l2_copy_gbs(local)
-    roofline["l2_copy_gbs"] = l2["gbs"]
-    roofline["frac_of_l2_copy"] = achieved / l2["gbs"]
+    for r in (trace_roof, shade_roof):
+        r["l2_copy_gbs"] = l2["gbs"]
+        r["frac_of_l2_copy"] = r["achieved"] / l2["gbs"]
     interior = spheres = None
     if rank == 0 and not args.no_interior:
         interior = run_scene_metric(ctx, 3, INTERIOR_WORKLOAD, hbm_peak, peak_src, l2["gbs"],
@@ -708,7 +757,8 @@ def run_gpu(args, world, rank, local, pg):
                                   f"{ws_mb:.0f} MB > 129 MB L2"),
                 "mrays_per_s": sum_over_ranks(pg, sum(s.ext_rays + s.shadow_rays for s in steps)) /
                                (ms_max * 1e-3) / 1e6,
-                "wall_s": wall, "clocks": clk.summary(), "roofline": roofline, "cpu_baseline": cpu,
+                "wall_s": wall, "clocks": clk.summary(), "roofline": roofline,
+                "stage_rooflines": {"k_trace_ext": trace_roof, "k_shade": shade_roof}, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_value, "unit": "Mpaths/s", "steps": args.steps,
                         "timing": "wall clock per step around scene upload + aqua_render + film download, "
                                   "L2 flushed before each step outside the timed stretch",
@@ -809,8 +859,8 @@ def main():
     # k_trace_ext launch (1M rays) of this workload, from `ncu --set full`
     # (40.53 MB read + 3.00 MB written, iteration 2 of a 16-spp render); every
     # launch of the step has the same queue size until the last samples drain.
-    ap.add_argument("--traffic-per-launch", type=float, default=43.53e6,
-                    help="DRAM bytes per k_trace_ext launch from an ncu capture")
+    ap.add_argument("--traffic-per-launch", type=float, default=0.0,
+                    help="DRAM bytes per k_trace_ext launch (default: the ncu figure per ray x rays per launch)")
     ap.add_argument("--spp", type=int, default=0,
                     help="samples per pixel of the workload (default 1024; smaller only for profiling captures)")
     ap.add_argument("--profile-scene", type=int, default=0, choices=[0, 2, 3, 5],

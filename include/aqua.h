@@ -126,20 +126,26 @@ typedef struct aqua_integrator_cfg {
 /* Launch shape of the wavefront. 0 in any field = the library default.
  * For a given `replicas` value every choice gives a bit-identical image: each
  * pixel (or, with replicas, each pixel's film copy) is owned by exactly one
- * path slot, which runs its samples in order. */
+ * path slot, which runs its samples in order. Automatic replicas aim at
+ * about 2^24 paths in flight (2^20 with the material sort and in the cache
+ * mode), so the automatic count can differ between sorted and unsorted
+ * renders of an image. */
 typedef struct aqua_tuning {
-    int32_t slots;          /* paths in flight (0 = one per pixel, capped)   */
+    int32_t slots;          /* paths in flight (0 = one per pixel, capped at
+                               2^24, or 2^20 sorted)                         */
     int32_t block_trace;    /* threads per block, traversal kernels          */
     int32_t block_shade;    /* threads per block, shading kernel             */
-    int32_t sort_by_material; /* 1 = bin hits by material before shading     */
+    int32_t sort_by_material; /* 1 = bin hits by material before shading
+                                 (default 0)                                 */
     int32_t blocks_per_sm;  /* persistent grid = SMs * this                  */
     int32_t use_graph;      /* 1 = replay iterations from a CUDA graph       */
     int32_t iters_per_graph;/* iterations between host checks of the queue  */
-    int32_t replicas;       /* sample replicas per pixel: 0 = automatic (small
-                               images get several slots per pixel, each with
-                               its own film copy), 1 = off, k = k copies     */
+    int32_t replicas;       /* sample replicas per pixel: 0 = automatic (images
+                               below the paths-in-flight target get several
+                               slots per pixel, each with its own film
+                               copy), 1 = off, k = k copies                  */
     int32_t kernel;         /* AQUA_KERNEL_*: the wavefront (three launches per
-                               bounce over compacted, material-sorted queues)
+                               bounce over compacted queues)
                                or one persistent launch whose lanes each keep a
                                path in flight and regenerate it in place (the
                                aqua_render_batch kernel; block_trace and

@@ -7,8 +7,9 @@ extension/shadow ray counts agree to within the rare FP32/FP64 divergences
 (2e-3 relative).
 
 - The Cornell GGX box at the bench's exact launch shape: 1024 x 1024 pixels,
-  2^20 path slots (one per pixel, no sample replicas), material-sorted
-  shading, default tuning — only the sample count is lowered.
+  2^24 path slots (16 sample replicas per pixel, each with its film copy),
+  unsorted shading, default tuning — only the samples per slot are lowered
+  (1 instead of 64).
 - The synthetic interior at 1920 x 1080 (2,073,600 slots, textures),
   against the FP32 oracle at 1 spp and the FP64 oracle at 32 spp.
 - One persistent-kernel batch job per scene of the 64-job serving batch,
@@ -48,12 +49,13 @@ def test_cornell_ggx_at_bench_shape(gpu_ctx):
     import pyoracle
 
     s = gpu_ctx.procedural(2, seed=0, width=1024, height=1024)
-    cfg = gpu_ctx.integrator(spp=2, max_depth=8, rr_depth=3, seed=1)
+    cfg = gpu_ctx.integrator(spp=16, max_depth=8, rr_depth=3, seed=1)
     img, st = gpu_ctx.render(s, cfg, tuning=gpu_ctx.tuning())
-    # the bench's shape: one slot per pixel, no replicas
-    assert gpu_ctx.workspace_bytes() > 150e6  # 2^20 slots of path state, queues and buckets
+    # the bench's shape: 16 slots per pixel (2^24 paths in flight)
+    assert st.iterations < 64  # one sample per slot: the queue drains within the bounce limit and its tail
+    assert gpu_ctx.workspace_bytes() > 2e9  # 2^24 slots of path state and queues
     o = pyoracle.OracleScene.from_aqua(s)
-    ref, ost = o.render(2, 8, seed=1, precision=64)
+    ref, ost = o.render(16, 8, seed=1, precision=64)
     err = rel_mse(img, ref)
     assert err < TOL, err
     check_counts(st, ost)

@@ -80,7 +80,7 @@ def test_launch_shape_does_not_change_the_image(gpu_ctx):
 def test_sample_replicas(gpu_ctx):
     """Small images run several slots per pixel, each on its own film copy:
     deterministic for a given replica count, equal up to summation order
-    across counts, and the default for images below 2^20 pixels."""
+    across counts, and the default for images below 2^24 pixels."""
     import pyoracle
 
     s = gpu_ctx.procedural(2, seed=0, width=40, height=30)
