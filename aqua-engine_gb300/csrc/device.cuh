@@ -317,9 +317,13 @@ __device__ __forceinline__ TraceResult traverse_fast(const DevScene& S, v3 o, v3
 //                 round together (warp collectives inside are allowed).
 constexpr int kRefillLanes = 16;
 
-template <bool ANY, class Load, class Done>
-__device__ __forceinline__ void traverse_queue(const DevScene& S, uint32_t n, uint32_t* cursor, Load load,
-                                               Done done) {
+// Kinds of queue: closest hits, any hits, or both mixed (the load callback
+// then sets `any` per ray: load(i, o, d, tmin, tmax, any)).
+enum { kQueueClosest = 0, kQueueAny = 1, kQueueMixed = 2 };
+
+template <int KIND, class Load, class Done>
+__device__ __forceinline__ void traverse_queue_kind(const DevScene& S, uint32_t n, uint32_t* cursor, Load load,
+                                                    Done done) {
     const unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     RayPre rp;
@@ -329,7 +333,7 @@ __device__ __forceinline__ void traverse_queue(const DevScene& S, uint32_t n, ui
     int sp = 0;
     int32_t node = kTraversalDone, leaf = 0;
     uint32_t tag = 0;
-    bool have = false, drained = false;
+    bool have = false, drained = false, any = KIND == kQueueAny;
     while (true) {
         const unsigned idle = __ballot_sync(kFull, !have);
         if (!drained && idle != 0u && (__popc(idle) >= kRefillLanes || idle == kFull)) {
@@ -343,7 +347,8 @@ __device__ __forceinline__ void traverse_queue(const DevScene& S, uint32_t n, ui
                 if (i < n) {
                     v3 o, d;
                     float tmin, tmax;
-                    tag = load(i, o, d, tmin, tmax);
+                    if constexpr (KIND == kQueueMixed) tag = load(i, o, d, tmin, tmax, any);
+                    else tag = load(i, o, d, tmin, tmax);
                     rp.o = o;
                     rp.invd = mk(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
                     rp.tmin = tmin;
@@ -379,7 +384,7 @@ __device__ __forceinline__ void traverse_queue(const DevScene& S, uint32_t n, ui
                                          rp.tmax);
                 if (h.hit) {
                     int32_t id = __float_as_int(a.w);
-                    if (ANY) {
+                    if (KIND == kQueueAny || (KIND == kQueueMixed && any)) {
                         r.t = h.t; r.tri = first + k; r.id = id;
                         stop = true;
                         break;
@@ -404,6 +409,12 @@ __device__ __forceinline__ void traverse_queue(const DevScene& S, uint32_t n, ui
             have = false;
         }
     }
+}
+
+template <bool ANY, class Load, class Done>
+__device__ __forceinline__ void traverse_queue(const DevScene& S, uint32_t n, uint32_t* cursor, Load load,
+                                               Done done) {
+    traverse_queue_kind<ANY ? kQueueAny : kQueueClosest>(S, n, cursor, load, done);
 }
 
 // Warp-aggregated append: lanes with pred set get consecutive slots of *ctr.

@@ -190,7 +190,7 @@ struct BatchGraph {
     uint32_t units = 0;
 };
 
-enum { kCntQ0 = 0, kCntQ1 = 1, kCntShadow = 2, kCntBucket0 = 8 };
+enum { kCntQ0 = 0, kCntQ1 = 1, kCntShadow = 2, kCntBucket0 = 10 };
 enum { kStatExt = 0, kStatShadow, kStatPaths, kStatNodes, kStatTris, kStatShNodes, kStatShTris, kStatCount };
 
 }  // namespace aq
