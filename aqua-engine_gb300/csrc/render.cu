@@ -365,7 +365,10 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
         int32_t tri = __float_as_int(h.w);
         if (tri < 0) {
             v3 e = mk(S.env[0], S.env[1], S.env[2]);
-            if (e.x > 0.0f || e.y > 0.0f || e.z > 0.0f) film_add(W.film, pixel, thr * e);
+            if (e.x > 0.0f || e.y > 0.0f || e.z > 0.0f) {
+                if (!NRC || (int)depth <= P.max_depth) film_add(W.film, pixel, thr * e);
+                if (NRC && tag) ltrain_add(W.ltrain, train_id, thr * e);
+            }
         } else {
             float4 rd = W.ray_d[s];
             const float4* tw = S.tris + 3 * (size_t)tri;
@@ -387,7 +390,10 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                         float pl = L.e2.w * h.x * h.x / (L.e1.w * cos_l);
                         w = power_heuristic(pdf_b, pl);
                     }
-                    if (!(NRC && P.visualize)) film_add(W.film, pixel, thr * f3(L.le) * w);
+                    // Past max_depth a training path gathers for its targets only:
+                    // the image keeps the plain estimator's depth.
+                    if (!(NRC && P.visualize) && (!NRC || (int)depth <= P.max_depth))
+                        film_add(W.film, pixel, thr * f3(L.le) * w);
                     if (NRC && tag) ltrain_add(W.ltrain, train_id, thr * f3(L.le) * w);
                 }
             }
@@ -516,8 +522,12 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                         v3 so = offset_ray(p, below ? -ng : ng);
                         W.sh_o[k] = make_float4(so.x, so.y, so.z, __int_as_float((int)pixel));
                         W.sh_d[k] = make_float4(wi.x, wi.y, wi.z, dist * (1.0f - 1e-4f));
-                        W.sh_c[k] = make_float4(contrib.x, contrib.y, contrib.z,
-                                                __int_as_float(NRC && tag ? (int)(train_id + 1u) : 0));
+                        // w: 0, or the training path's id + 1 (negated: its
+                        // targets only, the bounce lies past max_depth)
+                        const int tid = NRC && tag ? ((int)depth < P.max_depth ? (int)(train_id + 1u)
+                                                                                : -(int)(train_id + 1u))
+                                                   : 0;
+                        W.sh_c[k] = make_float4(contrib.x, contrib.y, contrib.z, __int_as_float(tid));
                     }
                 }
                 // BSDF sampling.
@@ -571,11 +581,9 @@ __device__ __forceinline__ void shadow_done(const WaveParams& P, const WavePtrs&
     if (r.tri < 0) {
         float4 c = W.sh_c[i];
         uint32_t pixel = (uint32_t)__float_as_int(W.sh_o[i].w);
-        if (!(NRC && P.visualize)) film_add(W.film, pixel, mk(c.x, c.y, c.z));
-        if (NRC) {
-            int id = __float_as_int(c.w);
-            if (id > 0) ltrain_add(W.ltrain, (uint32_t)(id - 1), mk(c.x, c.y, c.z));
-        }
+        const int id = __float_as_int(c.w);  // training path id + 1, negated past max_depth
+        if (!(NRC && P.visualize) && id >= 0) film_add(W.film, pixel, mk(c.x, c.y, c.z));
+        if (NRC && id != 0) ltrain_add(W.ltrain, (uint32_t)((id > 0 ? id : -id) - 1), mk(c.x, c.y, c.z));
     }
 }
 
