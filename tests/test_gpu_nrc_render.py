@@ -57,6 +57,25 @@ def test_zero_cache_equals_truncated_path_tracer(gpu_ctx):
     s.free()
 
 
+def test_training_paths_keep_the_plain_depth_in_the_image(gpu_ctx):
+    """When every path is a training path nothing queries the cache, and
+    what the paths gather past max_depth (they run on for their targets)
+    must stay out of the image: it equals the plain path tracer's, with the
+    same random numbers, bit for bit."""
+    import aqua
+
+    s = gpu_ctx.procedural(2, seed=0, width=48, height=40)
+    net = aqua.Nrc(gpu_ctx, seed=1)
+    tune = gpu_ctx.tuning(replicas=4)
+    cfg = nrc_cfg(gpu_ctx, spp=4, seed=5, nrc_query_vertex=aqua.NRC_QUERY_SPREAD, nrc_train_samples=1 << 20)
+    img, st = gpu_ctx.render_nrc(s, cfg, net, tuning=tune)
+    ref, _ = gpu_ctx.render(s, gpu_ctx.integrator(spp=4, max_depth=8, rr_depth=3, seed=5), tuning=tune)
+    assert st.nrc_queries == 0 and st.nrc_train_records > 48 * 40 * 4
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    net.free()
+    s.free()
+
+
 @pytest.mark.parametrize("config", [1, 2])
 def test_constant_cache_matches_oracle(gpu_ctx, config):
     import aqua
