@@ -39,7 +39,8 @@ struct WaveParams {
     uint32_t max_train_paths;  // capacity of the per-training-path accumulators
     uint32_t max_records;      // capacity of the training-vertex records
     int32_t train_span;        // reflections a target covers: max_depth - query_depth
-    int32_t train_depth;       // bounce limit of training paths: max_depth + train_span
+    int32_t record_depth;      // training paths record their vertices at bounces below this
+    int32_t train_depth;       // bounce limit of training paths: record_depth + train_span
     int32_t visualize;         // 1 = the image is the cache seen at the first hit
     // Sample replicas (0 or 1 = off). With K > 1 there are K slots per pixel:
     // slot s = r * pixels + p runs samples r, r + K, r + 2K, ... of pixel p
@@ -452,7 +453,7 @@ __global__ void __launch_bounds__(128, 6) k_shade(DevScene S, WaveParams P, Wave
                     } else if (tag) {
                         float4 lb = W.ltrain[train_id];
                         W.lsnap[(size_t)train_id * (size_t)P.train_depth + depth] = lb;
-                        uint32_t k = (int)depth < P.max_depth ? atomicAdd(&W.counters[kCntRecord], 1u) : 0xffffffffu;
+                        uint32_t k = (int)depth < P.record_depth ? atomicAdd(&W.counters[kCntRecord], 1u) : 0xffffffffu;
                         if (k < P.max_records) {
                             float r[24];
                             nrc_raw(r, p, wo, ns, m.b.y, kd, B.F0);
@@ -1054,6 +1055,9 @@ __global__ void k_nrc_targets(const float4* __restrict__ rec, uint32_t n, const 
     }
 }
 
+// Vertices a training path records in path-spread mode (bounces 0..3).
+constexpr int kSpreadRecordDepth = 4;
+
 static void ensure_nrc_workspace(aqua_ctx* ctx, size_t queries, size_t records, size_t snaps) {
     NrcWorkspace& w = ctx->nrc_ws;
     if (w.block.ptr && w.queries >= queries && w.records >= records && w.snaps >= snaps) return;
@@ -1115,7 +1119,13 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     const bool by_spread = !cfg.visualize_cache && cfg.nrc_query_vertex == AQUA_NRC_QUERY_SPREAD;
     const int query_depth = cfg.visualize_cache ? 0 : by_spread ? -1 : std::max(0, cfg.nrc_query_vertex - 1);
     const int train_span = std::max(1, cfg.max_depth - (by_spread ? 1 : query_depth));
-    const int train_depth = std::min(cfg.max_depth + train_span, 250);
+    // By path spread most queries fall on vertices 2-4, so training paths
+    // record their first four vertices only and end train_span bounces past
+    // the fourth: shorter tails of the few-ray iterations that follow the
+    // queries. With a fixed query vertex they record every vertex below
+    // max_depth.
+    const int record_depth = by_spread ? std::min(cfg.max_depth, kSpreadRecordDepth) : cfg.max_depth;
+    const int train_depth = std::min(record_depth + train_span, 250);
     ensure_nrc_workspace(ctx, cap_q, cap_r, (size_t)train_depth);
     Workspace& w = ctx->ws;
     NrcWorkspace& nw = ctx->nrc_ws;
@@ -1151,6 +1161,7 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     P.max_train_paths = (uint32_t)cap_r;
     P.max_records = (uint32_t)cap_r;
     P.train_span = train_span;
+    P.record_depth = record_depth;
     P.train_depth = train_depth;
     P.visualize = visualize ? 1 : 0;
     WavePtrs W{};
@@ -1195,7 +1206,9 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
         AQ_CUDA(cudaGetLastError());
         ++launches;
     }
-    const int chunk = tune.iters_per_graph > 0 ? tune.iters_per_graph : 16;
+    // A 1-spp frame drains within train_depth + 1 iterations: no empty
+    // iterations before the host's check.
+    const int chunk = tune.iters_per_graph > 0 ? tune.iters_per_graph : std::min(16, train_depth + 2);
     const uint64_t max_iters =
         (uint64_t)(train_depth + 2) * (uint64_t)cfg.spp * ((pixels + slots - 1) / slots) + 64;
     uint64_t iter = 0;
