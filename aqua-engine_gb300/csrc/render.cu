@@ -1208,7 +1208,7 @@ void render_nrc(aqua_ctx* ctx, aqua_scene* sc, const aqua_integrator_cfg& cfg, c
     }
     // A 1-spp frame drains within train_depth + 1 iterations: no empty
     // iterations before the host's check.
-    const int chunk = tune.iters_per_graph > 0 ? tune.iters_per_graph : std::min(16, train_depth + 2);
+    const int chunk = std::min(tune.iters_per_graph > 0 ? tune.iters_per_graph : 16, train_depth + 2);
     const uint64_t max_iters =
         (uint64_t)(train_depth + 2) * (uint64_t)cfg.spp * ((pixels + slots - 1) / slots) + 64;
     uint64_t iter = 0;
