@@ -7,6 +7,9 @@
 //                 BSDF sampling, Russian roulette; a finished path is replaced
 //                 in place by the slot's next camera sample (ray generation)
 //   k_shadow      any-hit test of the shadow queue, film += unoccluded NEE
+// (In the cache mode k_trace_fused walks an iteration's extension rays and
+// the previous iteration's shadow rays in one launch, two launches per
+// iteration.) Renders keep about 2^24 paths in flight (sample replicas).
 // Path slot s owns pixels s, s + S, s + 2S, ... and runs their samples in
 // order, so film updates need no atomics and the image does not depend on
 // the launch shape, the slot count or the material sort.
