@@ -690,6 +690,10 @@ def run_gpu(args, world, rank, local, pg):
                   "note": f"algorithmic bytes = {SHADE_BYTES_PER_PATH} B per shaded path (queue entry, path state, "
                           "hit, direction, triangle, material read; path state and next-queue entry written) + "
                           f"{SHADOW_RECORD_BYTES} B per shadow record written"}
+    for r in (trace_roof, shade_roof):  # DRAM rate implied by the traffic figure
+        if r["traffic"]:
+            r["dram_gbs"] = r["traffic"] / (r["avg_launch_us"] * 1e-6) / 1e9
+            r["dram_frac"] = r["dram_gbs"] / hbm_peak
     roofline = shade_roof if staged.shade_ms >= staged.trace_ms else trace_roof
 
     # End to end through the C ABI with host buffers: scene upload from
